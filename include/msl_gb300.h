@@ -1,0 +1,183 @@
+/*
+ * msl_gb300.h -- C ABI of the GB300 skeleton library (libmsl_gb300.so).
+ *
+ * The Muesli reference (NinaHerrmann/muesli4) is a header-only C++ template
+ * API with no C ABI; this header is the boundary its skeleton hot path would
+ * bind through an FFI. Every entry point names the reference function it
+ * replaces (path:line inside the reference project).
+ *
+ * Conventions
+ *  - Every function returns an int status: MSL_OK (0) or a negative MSL_ERR_*.
+ *    The reference prints exceptions and continues (src/muesli.cpp:292-294) or
+ *    exit()s on CUDA errors (include/muesli.h:70-77); this ABI never exits and
+ *    never throws. msl_last_error_string() describes the last failure of the
+ *    calling thread.
+ *  - Device pointers are plain addresses in the memory of the current device
+ *    (msl_alloc, or any cudaMalloc'd buffer). Host pointers are plain host
+ *    memory; pinned memory makes the copies faster but is not required.
+ *  - All device work is enqueued on the library stream (msl_get_stream /
+ *    msl_set_stream). Calls that return a value to the host (folds, residuals)
+ *    synchronise that stream; the others return once the work is enqueued.
+ *  - Element types: MSL_F32 (float), MSL_F64 (double), MSL_I32 (int32,
+ *    two's-complement wrap-around arithmetic), MSL_BF16 (bfloat16 storage,
+ *    stencils only).
+ *  - Layouts (one partition, the whole container): DA is T[n]; DM is
+ *    row-major T[rows][cols] (include/dm.h); DC is T[depth][rows][cols], index
+ *    (z*rows + y)*cols + x (include/plcube.h:121-123).
+ */
+#ifndef MSL_GB300_H
+#define MSL_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (names follow include/detail/exception.h) ------------- */
+#define MSL_OK 0
+#define MSL_ERR_INVALID_ARGUMENT (-1)   /* IllegalArgument / IllegalFunctorException */
+#define MSL_ERR_NOT_INITIALIZED (-2)    /* MissingInitializationException */
+#define MSL_ERR_CUDA (-3)               /* a CUDA runtime/driver call failed */
+#define MSL_ERR_OUT_OF_MEMORY (-4)      /* DeviceOutOfMemory */
+#define MSL_ERR_NOT_IMPLEMENTED (-5)    /* NotYetImplementedException */
+#define MSL_ERR_SIZE_MISMATCH (-6)      /* SizeMismatch / NotSameSizeException / InvalidCube */
+#define MSL_ERR_TIMEOUT (-7)            /* a bounded device-side wait gave up */
+#define MSL_ERR_BUDGET (-8)             /* HBM budget of a batch/server exceeded */
+#define MSL_ERR_UNSUPPORTED_DEVICE (-9) /* FeatureNotSupportedByDeviceException */
+
+/* ---- element types ------------------------------------------------------- */
+#define MSL_F32 0
+#define MSL_F64 1
+#define MSL_I32 2
+#define MSL_BF16 3
+
+/* ---- built-in map functors: out = op(x) ---------------------------------- */
+#define MSL_MAP_AFFINE 0   /* p[0]*x + p[1]  (two roundings, never fused) */
+#define MSL_MAP_ABS 1      /* |x| */
+#define MSL_MAP_SQUARE 2   /* x*x */
+
+/* ---- built-in zip functors: out = op(a, b) ------------------------------- */
+#define MSL_ZIP_ADD 0      /* a + b */
+#define MSL_ZIP_SUB 1      /* a - b */
+#define MSL_ZIP_MUL 2      /* a * b */
+#define MSL_ZIP_MULADD 3   /* a*b + a (two roundings) */
+#define MSL_ZIP_ABSDIFF 4  /* |a - b| */
+#define MSL_ZIP_MAX 5      /* a > b ? a : b */
+#define MSL_ZIP_MIN 6      /* a < b ? a : b */
+/* three-input zip (msl_zip3): out = op(a, b, c) */
+#define MSL_ZIP3_MULADD 0  /* a*b + c (two roundings) */
+#define MSL_ZIP3_SUM 1     /* (a + b) + c */
+
+/* ---- built-in index functors ----------------------------------------------
+ * Coordinates c[] in the reference's argument order: DA (i); DM (row, col);
+ * DC (x=col, y=row, z=depth). v is the element of the first input, w of the
+ * second (zip_index only).                                                  */
+#define MSL_IDX_LINEAR 0   /* p[0]*c0 + p[1]*c1 (+ p[2]*c2) + p[nd]*v (+ p[nd+1]*w), left to right */
+#define MSL_IDX_PRODUCT 1  /* c0 * c1 (* c2) * v (* w) */
+#define MSL_IDX_XOR_MASK 2 /* v ^ (flat_index & p[0])   (MSL_I32 only) */
+#define MSL_IDX_BORDER 3   /* DM/DC: row 0 -> p[0]; other boundary cells -> p[1]; inside -> v */
+
+/* ---- built-in fold functors ---------------------------------------------- */
+#define MSL_FOLD_SUM 0
+#define MSL_FOLD_MAX 1
+#define MSL_FOLD_MIN 2
+
+/* ---- built-in stencil functors --------------------------------------------
+ * view(x, y[, z]) is the input at that cell, or `neutral` outside the grid
+ * (include/nplmatrix.h:123-139, include/plcube.h:105-119).                 */
+#define MSL_ST2_JACOBI5 0  /* boundary cells keep view(x,y); inside: (((0+W)+E)+N)+S, /4 */
+#define MSL_ST2_HEAT5 1    /* every cell: (((0+W)+E)+N)+S, /4 (examples/heatdiffusion.cpp:67-76) */
+#define MSL_ST2_BOXMEAN 2  /* sum over dx outer, dy inner of view, / (2r+1)^2 */
+#define MSL_ST2_BOXSUM 3   /* same sum, not divided */
+#define MSL_ST2_LIFE 4     /* Conway's rule, 8 neighbours (examples/gameoflife.cpp:22-42); MSL_I32 */
+#define MSL_ST3_HEAT7 0    /* ((((((0+W)+E)+N)+S)+B)+F)/6 (examples/heatdiffusion.cpp:55-65) */
+#define MSL_ST3_BOXSUM 1   /* sum over dx, dy, dz (outer to inner) (examples/meanblur2.cpp:46-57) */
+#define MSL_ST3_BOXMEAN 2  /* the same sum / (2r+1)^3 (examples/meanblur20.cpp) */
+
+/* ---- runtime ------------------------------------------------------------- */
+/* Bind the calling process to `device`, create the library stream and the
+ * fold scratch. Replaces msl::initSkeletons (src/muesli.cpp:63-110). */
+int msl_init(int device);
+/* Release the stream and scratch. Replaces msl::terminateSkeletons (src/muesli.cpp:112-158). */
+int msl_terminate(void);
+/* Wait for all enqueued work. Replaces msl::syncStreams (src/muesli.cpp:213-223). */
+int msl_sync(void);
+/* Description of the calling thread's last error ("" if none). */
+const char *msl_last_error_string(void);
+/* Library stream as a cudaStream_t, and replacing it with a caller's stream
+ * (NULL restores the library's own). No reference counterpart: the reference
+ * keeps one stream per device in Muesli::streams (include/muesli.h:149-181). */
+int msl_get_stream(void **stream);
+int msl_set_stream(void *stream);
+/* Device facts: SM count, free and total device memory. */
+int msl_device_info(int *sm_count, size_t *free_bytes, size_t *total_bytes);
+/* Number of kernels this library has launched since msl_init. */
+int msl_launch_count(unsigned long long *count);
+
+/* ---- partition storage (DS<T>) ------------------------------------------- */
+/* Device partition of a container: DS ctor / initGPUs (src/ds.cpp:215-239). */
+int msl_alloc(void **dptr, size_t bytes);
+int msl_free(void *dptr);
+/* Host -> device: DS::updateDevice (src/ds.cpp:442-462), setLocalPartition (:274-287). */
+int msl_upload(void *dst_device, const void *src_host, size_t bytes);
+/* Device -> host: DS::updateHost / gather (src/ds.cpp:465-484, 539-591). Synchronous. */
+int msl_download(void *dst_host, const void *src_device, size_t bytes);
+/* Device -> device copy kernel: copyKernel (src/copy_kernel.cu:33-43), gather(DS&) (src/ds.cpp:562-581). */
+int msl_copy(void *dst_device, const void *src_device, size_t bytes);
+/* DS::fill(const T&) (src/ds.cpp:290-305). */
+int msl_fill(int dtype, void *dst, size_t n, double value);
+
+/* ---- element-wise skeletons --------------------------------------------- */
+/* out[i] = op(in[i]); in == out is mapInPlace.
+ * DS::map / mapInPlace (src/ds.cpp:614-663), mapKernel (src/map_kernels.cu:36-43). */
+int msl_map(int dtype, int op, const void *in, void *out, size_t n, const double *params);
+/* out[i] = op(a[i], b[i]); a == out is zipInPlace. The argument order is the
+ * reference GPU build's (src/zip_kernels.cu:37-43, launched src/ds.cpp:708-709).
+ * DS::zip / zipInPlace (src/ds.cpp:669-727). */
+int msl_zip(int dtype, int op, const void *a, const void *b, void *out, size_t n);
+/* out[i] = op(a[i], b[i], c[i]); DA::zipInPlace3 (src/da.cpp:434-459). */
+int msl_zip3(int dtype, int op, const void *a, const void *b, const void *c, void *out, size_t n);
+/* Index map: out = op(coords..., in). ndim 1: DA::mapIndex/mapIndexInPlace
+ * (src/da.cpp:232-255,328-355); ndim 2 (dims = rows, cols): DM::mapIndex*
+ * (src/dm.cpp:372-429); ndim 3 (dims = depth, rows, cols): DC::mapIndex*
+ * (src/dc.cpp:387-448). params holds up to 8 values. */
+int msl_map_index(int dtype, int op, const void *in, void *out, int ndim, const long long *dims,
+                  const double *params);
+/* Index zip: out = op(coords..., a, b). DA::zipIndex* (src/da.cpp:375-430),
+ * DM::zipIndex* (src/dm.cpp:435-501), DC::zipIndex* (src/dc.cpp:456-550),
+ * in the GPU build's argument order. */
+int msl_zip_index(int dtype, int op, const void *a, const void *b, void *out, int ndim,
+                  const long long *dims, const double *params);
+
+/* ---- folds ---------------------------------------------------------------- */
+/* *result (host, one element of dtype) = fold of in[0..n) with op, seeded with
+ * elements (no identity), single pass. n == 0 is MSL_ERR_INVALID_ARGUMENT.
+ * DS::fold / foldCPU (src/ds.cpp:741-954), foldKernel (src/fold_kernels.cu:51-129). */
+int msl_fold(int dtype, int op, const void *in, size_t n, void *result);
+/* *result = max_i |a[i] - b[i]| computed in FP64 (a zip + fold(max) fused in
+ * one pass; examples/jacobisolver.cpp:127-140 runs them as two skeletons). */
+int msl_fold_absdiff_max(int dtype, const void *a, const void *b, size_t n, double *result);
+
+/* ---- stencils ------------------------------------------------------------- */
+/* out = f(view, x, y) for every cell of a rows x cols grid; `radius` is the
+ * stencil size r, `neutral` the value outside the grid. in != out.
+ * DM::mapStencil<f> (src/dm.cpp:1535-1591), NPLMatrix (include/nplmatrix.h:56-168). */
+int msl_stencil2d(int dtype, int kind, const void *in, void *out, int rows, int cols, int radius,
+                  double neutral);
+/* `iters` ping-pong sweeps a -> b -> a ... (examples/heatdiffusion.cpp:93-96).
+ * On return *result_in_b says which buffer holds the last sweep; if residual is
+ * not NULL it receives max |last - previous| in FP64, fused into the last sweep. */
+int msl_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, int cols, int radius,
+                          double neutral, int iters, double *residual, int *result_in_b);
+/* 3-D: out = f(view, x, y, z) over depth x rows x cols.
+ * DC::mapStencil<f> (src/dc.cpp:559-592), PLCube (include/plcube.h:55-144). */
+int msl_stencil3d(int dtype, int kind, const void *in, void *out, int depth, int rows, int cols,
+                  int radius, double neutral);
+int msl_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int rows, int cols,
+                          int radius, double neutral, int iters, double *residual, int *result_in_b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MSL_GB300_H */

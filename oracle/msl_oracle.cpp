@@ -1,0 +1,502 @@
+// CPU oracle for the skeleton hot path -- TEST INFRASTRUCTURE, not product code.
+// See msl_oracle.h. Each function names the reference code whose loop it
+// restates (paths inside the Muesli reference project).
+#include "msl_oracle.h"
+
+#include <omp.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "../include/msl_gb300.h"
+
+namespace {
+
+// ---- bfloat16 storage (round to nearest even; NaN kept quiet) ---------------
+struct bf16 {
+    uint16_t bits;
+};
+inline float to_f(bf16 h) {
+    uint32_t u = (uint32_t)h.bits << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+inline bf16 from_f(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return bf16{(uint16_t)((u >> 16) | 0x40)};
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return bf16{(uint16_t)(u >> 16)};
+}
+
+// Scalar arithmetic with int32 wrap-around (the reference relies on the
+// two's-complement behaviour of its int functors).
+template <typename T> struct Ar {
+    static T add(T a, T b) { return a + b; }
+    static T sub(T a, T b) { return a - b; }
+    static T mul(T a, T b) { return a * b; }
+};
+template <> struct Ar<int32_t> {
+    static int32_t add(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+    static int32_t sub(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+    static int32_t mul(int32_t a, int32_t b) { return (int32_t)((uint32_t)a * (uint32_t)b); }
+};
+template <typename T> T absval(T x) { return x < 0 ? Ar<T>::sub(0, x) : x; }
+template <typename T> T param(const double *p, int k) { return p ? (T)p[k] : T(0); }
+template <> int32_t param<int32_t>(const double *p, int k) { return p ? (int32_t)(long long)p[k] : 0; }
+
+// ---- map: DS::map / mapInPlace, src/ds.cpp:614-663 --------------------------
+template <typename T>
+int map_t(int op, const T *in, T *out, size_t n, const double *p) {
+    const T a = param<T>(p, 0), b = param<T>(p, 1);
+    switch (op) {
+        case MSL_MAP_AFFINE:
+#pragma omp parallel for
+            for (long long k = 0; k < (long long)n; k++) out[k] = Ar<T>::add(Ar<T>::mul(a, in[k]), b);
+            return 0;
+        case MSL_MAP_ABS:
+#pragma omp parallel for
+            for (long long k = 0; k < (long long)n; k++) out[k] = absval(in[k]);
+            return 0;
+        case MSL_MAP_SQUARE:
+#pragma omp parallel for
+            for (long long k = 0; k < (long long)n; k++) out[k] = Ar<T>::mul(in[k], in[k]);
+            return 0;
+    }
+    return MSL_ERR_INVALID_ARGUMENT;
+}
+
+// ---- zip: DS::zip / zipInPlace, src/ds.cpp:669-727 (GPU argument order) -----
+template <typename T> T zip_op(int op, T a, T b) {
+    switch (op) {
+        case MSL_ZIP_ADD: return Ar<T>::add(a, b);
+        case MSL_ZIP_SUB: return Ar<T>::sub(a, b);
+        case MSL_ZIP_MUL: return Ar<T>::mul(a, b);
+        case MSL_ZIP_MULADD: return Ar<T>::add(Ar<T>::mul(a, b), a);
+        case MSL_ZIP_ABSDIFF: return absval(Ar<T>::sub(a, b));
+        case MSL_ZIP_MAX: return a > b ? a : b;
+        default: return a < b ? a : b;  // MSL_ZIP_MIN
+    }
+}
+template <typename T>
+int zip_t(int op, const T *a, const T *b, T *out, size_t n) {
+    if (op < MSL_ZIP_ADD || op > MSL_ZIP_MIN) return MSL_ERR_INVALID_ARGUMENT;
+#pragma omp parallel for
+    for (long long k = 0; k < (long long)n; k++) out[k] = zip_op<T>(op, a[k], b[k]);
+    return 0;
+}
+// DA::zipInPlace3, src/da.cpp:434-459.
+template <typename T>
+int zip3_t(int op, const T *a, const T *b, const T *c, T *out, size_t n) {
+    if (op != MSL_ZIP3_MULADD && op != MSL_ZIP3_SUM) return MSL_ERR_INVALID_ARGUMENT;
+#pragma omp parallel for
+    for (long long k = 0; k < (long long)n; k++)
+        out[k] = op == MSL_ZIP3_MULADD ? Ar<T>::add(Ar<T>::mul(a[k], b[k]), c[k])
+                                       : Ar<T>::add(Ar<T>::add(a[k], b[k]), c[k]);
+    return 0;
+}
+
+// ---- index functors ----------------------------------------------------------
+// Coordinates in the reference's argument order: DA f(i, ...) src/da.cpp:249;
+// DM f(row, col, ...) src/dm.cpp:393-395; DC f(col, row, depth, ...) via
+// mapIndexKernelDC src/map_kernels.cu:88-101.
+template <typename T>
+T index_op(int op, int nd, const long long *c, const long long *dims, long long flat, T v, T w,
+           bool has_w, const double *p) {
+    switch (op) {
+        case MSL_IDX_LINEAR: {
+            T acc = Ar<T>::mul(param<T>(p, 0), (T)c[0]);
+            for (int k = 1; k < nd; k++) acc = Ar<T>::add(acc, Ar<T>::mul(param<T>(p, k), (T)c[k]));
+            acc = Ar<T>::add(acc, Ar<T>::mul(param<T>(p, nd), v));
+            if (has_w) acc = Ar<T>::add(acc, Ar<T>::mul(param<T>(p, nd + 1), w));
+            return acc;
+        }
+        case MSL_IDX_PRODUCT: {
+            T acc = (T)c[0];
+            for (int k = 1; k < nd; k++) acc = Ar<T>::mul(acc, (T)c[k]);
+            acc = Ar<T>::mul(acc, v);
+            if (has_w) acc = Ar<T>::mul(acc, w);
+            return acc;
+        }
+        case MSL_IDX_XOR_MASK: {
+            int32_t m = (int32_t)(long long)(p ? p[0] : 0);
+            return (T)((int32_t)v ^ (int32_t)(flat & m));
+        }
+        default: {  // MSL_IDX_BORDER
+            bool top, edge;
+            if (nd == 1) {
+                top = c[0] == 0;
+                edge = c[0] == dims[0] - 1;
+            } else if (nd == 2) {  // (row, col), dims = rows, cols
+                top = c[0] == 0;
+                edge = c[0] == dims[0] - 1 || c[1] == 0 || c[1] == dims[1] - 1;
+            } else {  // (x, y, z), dims = depth, rows, cols
+                top = c[1] == 0;
+                edge = c[0] == 0 || c[0] == dims[2] - 1 || c[1] == dims[1] - 1 || c[2] == 0 ||
+                       c[2] == dims[0] - 1;
+            }
+            if (top) return param<T>(p, 0);
+            if (edge) return param<T>(p, 1);
+            return v;
+        }
+    }
+}
+
+template <typename T>
+int index_t(int op, const T *a, const T *b, T *out, int nd, const long long *dims, const double *p) {
+    if (nd < 1 || nd > 3 || op < MSL_IDX_LINEAR || op > MSL_IDX_BORDER) return MSL_ERR_INVALID_ARGUMENT;
+    long long n = 1;
+    for (int k = 0; k < nd; k++) n *= dims[k];
+#pragma omp parallel for
+    for (long long k = 0; k < n; k++) {
+        long long c[3];
+        if (nd == 1) {
+            c[0] = k;
+        } else if (nd == 2) {  // src/dm.cpp:393-394
+            c[0] = k / dims[1];
+            c[1] = k % dims[1];
+        } else {  // src/map_kernels.cu:92-96
+            long long layer = dims[1] * dims[2];
+            c[2] = k / layer;
+            long long rem = k % layer;
+            c[1] = rem / dims[2];
+            c[0] = rem % dims[2];
+        }
+        out[k] = index_op<T>(op, nd, c, dims, k, a[k], b ? b[k] : T(0), b != nullptr, p);
+    }
+    return 0;
+}
+
+// ---- fold: DS::foldCPU, src/ds.cpp:924-954 -----------------------------------
+// A left fold seeded with the first element, run on one thread (the
+// reference's omp-parallel version of this loop is a data race).
+template <typename T>
+int fold_t(int op, const T *in, size_t n, T *res) {
+    if (n == 0 || op < MSL_FOLD_SUM || op > MSL_FOLD_MIN) return MSL_ERR_INVALID_ARGUMENT;
+    T acc = in[0];
+    for (size_t k = 1; k < n; k++) {
+        T x = in[k];
+        if (op == MSL_FOLD_SUM) acc = Ar<T>::add(acc, x);
+        else if (op == MSL_FOLD_MAX) acc = acc > x ? acc : x;
+        else acc = acc < x ? acc : x;
+    }
+    *res = acc;
+    return 0;
+}
+
+// ---- stencil views -------------------------------------------------------------
+// NPLMatrix::operator() on one partition, include/nplmatrix.h:123-139.
+template <typename S> struct View2 {
+    const S *d;
+    int width, height;
+    float neutral_f;
+    S neutral;
+    float operator()(int x, int y) const {
+        if (x < 0 || y < 0 || x >= width || y >= height) return neutral_f;
+        return (float)d[(long long)y * width + x];
+    }
+};
+template <> struct View2<bf16> {
+    const bf16 *d;
+    int width, height;
+    float neutral_f;
+    bf16 neutral;
+    float operator()(int x, int y) const {
+        if (x < 0 || y < 0 || x >= width || y >= height) return neutral_f;
+        return to_f(d[(long long)y * width + x]);
+    }
+};
+struct View2i {
+    const int32_t *d;
+    int width, height;
+    int32_t neutral;
+    int32_t operator()(int x, int y) const {
+        if (x < 0 || y < 0 || x >= width || y >= height) return neutral;
+        return d[(long long)y * width + x];
+    }
+};
+// PLCube::operator() on one partition, include/plcube.h:105-119.
+template <typename V> struct View3 {
+    const V *d;
+    int width, height, depth;
+    V neutral;
+    V operator()(int x, int y, int z) const {
+        if (x < 0 || y < 0 || z < 0 || x >= width || y >= height || z >= depth) return neutral;
+        return d[((long long)z * height + y) * width + x];
+    }
+};
+
+// The built-in 2-D functors, evaluated as their reference counterparts are.
+template <typename V, typename A>
+A stencil2_value(int kind, const V &m, int x, int y, int r) {
+    switch (kind) {
+        case MSL_ST2_JACOBI5:
+            if (x == 0 || y == 0 || x == m.width - 1 || y == m.height - 1) return m(x, y);
+            /* fall through */
+        case MSL_ST2_HEAT5: {  // examples/heatdiffusion.cpp:67-76
+            A v = 0;
+            v += m(x - 1, y);
+            v += m(x + 1, y);
+            v += m(x, y - 1);
+            v += m(x, y + 1);
+            v /= 4;
+            return v;
+        }
+        case MSL_ST2_BOXMEAN:
+        case MSL_ST2_BOXSUM: {  // loop nest of examples/meanblur2.cpp:46-57, in 2-D
+            A res = 0;
+            for (int mx = x - r; mx <= x + r; mx++)
+                for (int my = y - r; my <= y + r; my++) res += m(mx, my);
+            if (kind == MSL_ST2_BOXMEAN) res = res / (A)((2 * r + 1) * (2 * r + 1));
+            return res;
+        }
+    }
+    return 0;
+}
+// examples/gameoflife.cpp:22-42 on the NPLMatrix view.
+inline int32_t life_value(const View2i &m, int x, int y) {
+    int32_t sum = m(x, y - 1) + m(x - 1, y - 1) + m(x + 1, y - 1) + m(x, y + 1) + m(x - 1, y + 1) +
+                  m(x + 1, y + 1) + m(x - 1, y) + m(x + 1, y);
+    int32_t alive = m(x, y);
+    int32_t next = 0;
+    if (alive == 1 && (sum == 2 || sum == 3)) next = 1;
+    if (alive == 0 && sum == 3) next = 1;
+    return next;
+}
+
+inline bool kind2_ok(int dtype, int kind) {
+    if (dtype == MSL_I32) return kind == MSL_ST2_LIFE;
+    if (dtype == MSL_BF16) return kind == MSL_ST2_JACOBI5 || kind == MSL_ST2_HEAT5;
+    return kind >= MSL_ST2_JACOBI5 && kind <= MSL_ST2_BOXSUM;
+}
+
+// DM::mapStencil<f>, src/dm.cpp:1578-1590, with the functor called as
+// f(view, x=col, y=row) (the GPU build's convention, include/detail/map_kernels.cuh:159-168).
+int stencil2d_any(int dtype, int kind, const void *in, void *out, int rows, int cols, int r,
+                  double neutral) {
+    long long n = (long long)rows * cols;
+    if (dtype == MSL_I32) {
+        View2i m{(const int32_t *)in, cols, rows, (int32_t)(long long)neutral};
+        int32_t *o = (int32_t *)out;
+#pragma omp parallel for
+        for (long long k = 0; k < n; k++) o[k] = life_value(m, (int)(k % cols), (int)(k / cols));
+    } else if (dtype == MSL_F32) {
+        View2<float> m{(const float *)in, cols, rows, (float)neutral, (float)neutral};
+        float *o = (float *)out;
+#pragma omp parallel for
+        for (long long k = 0; k < n; k++)
+            o[k] = stencil2_value<View2<float>, float>(kind, m, (int)(k % cols), (int)(k / cols), r);
+    } else if (dtype == MSL_BF16) {  // BF16 storage, FP32 arithmetic
+        View2<bf16> m{(const bf16 *)in, cols, rows, (float)neutral, from_f((float)neutral)};
+        bf16 *o = (bf16 *)out;
+#pragma omp parallel for
+        for (long long k = 0; k < n; k++)
+            o[k] = from_f(stencil2_value<View2<bf16>, float>(kind, m, (int)(k % cols), (int)(k / cols), r));
+    } else {  // MSL_F64
+        struct V {
+            const double *d;
+            int width, height;
+            double neutral;
+            double operator()(int x, int y) const {
+                if (x < 0 || y < 0 || x >= width || y >= height) return neutral;
+                return d[(long long)y * width + x];
+            }
+        } m{(const double *)in, cols, rows, neutral};
+        double *o = (double *)out;
+#pragma omp parallel for
+        for (long long k = 0; k < n; k++)
+            o[k] = stencil2_value<V, double>(kind, m, (int)(k % cols), (int)(k / cols), r);
+    }
+    return 0;
+}
+
+template <typename V, typename A>
+A stencil3_value(int kind, const V &c, int x, int y, int z, int r) {
+    if (kind == MSL_ST3_HEAT7) {  // examples/heatdiffusion.cpp:55-65
+        A v = 0;
+        v += c(x - 1, y, z);
+        v += c(x + 1, y, z);
+        v += c(x, y - 1, z);
+        v += c(x, y + 1, z);
+        v += c(x, y, z - 1);
+        v += c(x, y, z + 1);
+        v /= 6;
+        return v;
+    }
+    A res = 0;  // examples/meanblur2.cpp:46-57
+    for (int mx = x - r; mx <= x + r; mx++)
+        for (int my = y - r; my <= y + r; my++)
+            for (int mz = z - r; mz <= z + r; mz++) res += c(mx, my, mz);
+    if (kind == MSL_ST3_BOXMEAN) res = res / (A)((2 * r + 1) * (2 * r + 1) * (2 * r + 1));
+    return res;
+}
+
+// DC::mapStencil<f>, src/dc.cpp:578-590.
+int stencil3d_any(int dtype, int kind, const void *in, void *out, int depth, int rows, int cols, int r,
+                  double neutral) {
+    long long layer = (long long)rows * cols, n = layer * depth;
+    if (dtype == MSL_F32) {
+        View3<float> c{(const float *)in, cols, rows, depth, (float)neutral};
+        float *o = (float *)out;
+#pragma omp parallel for
+        for (long long k = 0; k < n; k++) {
+            int z = (int)(k / layer), y = (int)((k % layer) / cols), x = (int)(k % cols);
+            o[k] = stencil3_value<View3<float>, float>(kind, c, x, y, z, r);
+        }
+    } else {
+        View3<double> c{(const double *)in, cols, rows, depth, neutral};
+        double *o = (double *)out;
+#pragma omp parallel for
+        for (long long k = 0; k < n; k++) {
+            int z = (int)(k / layer), y = (int)((k % layer) / cols), x = (int)(k % cols);
+            o[k] = stencil3_value<View3<double>, double>(kind, c, x, y, z, r);
+        }
+    }
+    return 0;
+}
+
+size_t dsize(int dtype) {
+    switch (dtype) {
+        case MSL_F32: case MSL_I32: return 4;
+        case MSL_F64: return 8;
+        case MSL_BF16: return 2;
+    }
+    return 0;
+}
+double as_double(int dtype, const void *p, long long k) {
+    switch (dtype) {
+        case MSL_F32: return ((const float *)p)[k];
+        case MSL_F64: return ((const double *)p)[k];
+        case MSL_I32: return ((const int32_t *)p)[k];
+        default: return to_f(((const bf16 *)p)[k]);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_set_threads(int n) {
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+}
+
+int oracle_map(int dtype, int op, const void *in, void *out, size_t n, const double *p) {
+    switch (dtype) {
+        case MSL_F32: return map_t<float>(op, (const float *)in, (float *)out, n, p);
+        case MSL_F64: return map_t<double>(op, (const double *)in, (double *)out, n, p);
+        case MSL_I32: return map_t<int32_t>(op, (const int32_t *)in, (int32_t *)out, n, p);
+    }
+    return MSL_ERR_INVALID_ARGUMENT;
+}
+
+int oracle_zip(int dtype, int op, const void *a, const void *b, void *out, size_t n) {
+    switch (dtype) {
+        case MSL_F32: return zip_t<float>(op, (const float *)a, (const float *)b, (float *)out, n);
+        case MSL_F64: return zip_t<double>(op, (const double *)a, (const double *)b, (double *)out, n);
+        case MSL_I32: return zip_t<int32_t>(op, (const int32_t *)a, (const int32_t *)b, (int32_t *)out, n);
+    }
+    return MSL_ERR_INVALID_ARGUMENT;
+}
+
+int oracle_zip3(int dtype, int op, const void *a, const void *b, const void *c, void *out, size_t n) {
+    switch (dtype) {
+        case MSL_F32:
+            return zip3_t<float>(op, (const float *)a, (const float *)b, (const float *)c, (float *)out, n);
+        case MSL_F64:
+            return zip3_t<double>(op, (const double *)a, (const double *)b, (const double *)c, (double *)out, n);
+        case MSL_I32:
+            return zip3_t<int32_t>(op, (const int32_t *)a, (const int32_t *)b, (const int32_t *)c,
+                                   (int32_t *)out, n);
+    }
+    return MSL_ERR_INVALID_ARGUMENT;
+}
+
+int oracle_map_index(int dtype, int op, const void *in, void *out, int nd, const long long *dims,
+                     const double *p) {
+    if (op == MSL_IDX_XOR_MASK && dtype != MSL_I32) return MSL_ERR_INVALID_ARGUMENT;
+    switch (dtype) {
+        case MSL_F32: return index_t<float>(op, (const float *)in, nullptr, (float *)out, nd, dims, p);
+        case MSL_F64: return index_t<double>(op, (const double *)in, nullptr, (double *)out, nd, dims, p);
+        case MSL_I32: return index_t<int32_t>(op, (const int32_t *)in, nullptr, (int32_t *)out, nd, dims, p);
+    }
+    return MSL_ERR_INVALID_ARGUMENT;
+}
+
+int oracle_zip_index(int dtype, int op, const void *a, const void *b, void *out, int nd,
+                     const long long *dims, const double *p) {
+    if (op == MSL_IDX_XOR_MASK || op == MSL_IDX_BORDER) return MSL_ERR_INVALID_ARGUMENT;
+    switch (dtype) {
+        case MSL_F32: return index_t<float>(op, (const float *)a, (const float *)b, (float *)out, nd, dims, p);
+        case MSL_F64:
+            return index_t<double>(op, (const double *)a, (const double *)b, (double *)out, nd, dims, p);
+        case MSL_I32:
+            return index_t<int32_t>(op, (const int32_t *)a, (const int32_t *)b, (int32_t *)out, nd, dims, p);
+    }
+    return MSL_ERR_INVALID_ARGUMENT;
+}
+
+int oracle_fold(int dtype, int op, const void *in, size_t n, void *result) {
+    switch (dtype) {
+        case MSL_F32: return fold_t<float>(op, (const float *)in, n, (float *)result);
+        case MSL_F64: return fold_t<double>(op, (const double *)in, n, (double *)result);
+        case MSL_I32: return fold_t<int32_t>(op, (const int32_t *)in, n, (int32_t *)result);
+    }
+    return MSL_ERR_INVALID_ARGUMENT;
+}
+
+int oracle_fold_absdiff_max(int dtype, const void *a, const void *b, size_t n, double *result) {
+    if (n == 0 || dsize(dtype) == 0) return MSL_ERR_INVALID_ARGUMENT;
+    double m = 0.0;
+    for (size_t k = 0; k < n; k++) {
+        double d = std::fabs(as_double(dtype, a, (long long)k) - as_double(dtype, b, (long long)k));
+        if (d > m || d != d) m = d;
+    }
+    *result = m;
+    return 0;
+}
+
+int oracle_stencil2d(int dtype, int kind, const void *in, void *out, int rows, int cols, int r,
+                     double neutral) {
+    if (rows <= 0 || cols <= 0 || r < 0 || !kind2_ok(dtype, kind)) return MSL_ERR_INVALID_ARGUMENT;
+    return stencil2d_any(dtype, kind, in, out, rows, cols, r, neutral);
+}
+
+int oracle_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, int cols, int r,
+                             double neutral, int iters, double *residual, int *result_in_b) {
+    if (rows <= 0 || cols <= 0 || r < 0 || iters < 1 || !kind2_ok(dtype, kind)) return MSL_ERR_INVALID_ARGUMENT;
+    void *p = a, *q = b;
+    for (int i = 0; i < iters; i++) {
+        stencil2d_any(dtype, kind, p, q, rows, cols, r, neutral);
+        void *t = p; p = q; q = t;
+    }
+    if (result_in_b) *result_in_b = (p == b);
+    if (residual) oracle_fold_absdiff_max(dtype, p, q, (size_t)rows * cols, residual);
+    return 0;
+}
+
+int oracle_stencil3d(int dtype, int kind, const void *in, void *out, int depth, int rows, int cols,
+                     int r, double neutral) {
+    if (depth <= 0 || rows <= 0 || cols <= 0 || r < 0 || (dtype != MSL_F32 && dtype != MSL_F64) ||
+        kind < MSL_ST3_HEAT7 || kind > MSL_ST3_BOXMEAN)
+        return MSL_ERR_INVALID_ARGUMENT;
+    return stencil3d_any(dtype, kind, in, out, depth, rows, cols, r, neutral);
+}
+
+int oracle_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int rows, int cols,
+                             int r, double neutral, int iters, double *residual, int *result_in_b) {
+    if (iters < 1) return MSL_ERR_INVALID_ARGUMENT;
+    void *p = a, *q = b;
+    for (int i = 0; i < iters; i++) {
+        int rc = oracle_stencil3d(dtype, kind, p, q, depth, rows, cols, r, neutral);
+        if (rc) return rc;
+        void *t = p; p = q; q = t;
+    }
+    if (result_in_b) *result_in_b = (p == b);
+    if (residual) oracle_fold_absdiff_max(dtype, p, q, (size_t)depth * rows * cols, residual);
+    return 0;
+}
+
+}  // extern "C"

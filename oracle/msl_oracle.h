@@ -1,0 +1,47 @@
+/*
+ * CPU oracle for the skeleton hot path -- TEST INFRASTRUCTURE, not product code.
+ *
+ * A plain C++/OpenMP restatement of the Muesli reference's OpenMP (CPU) build
+ * of DA/DM/DC map, zip, index map/zip, fold and DM/DC mapStencil, with the
+ * built-in functors of include/msl_gb300.h. Only tests, the smoke check and
+ * the CPU-baseline leg of the benchmark load it (liboracle.so, via ctypes);
+ * the product library never does.
+ *
+ * Parity is pinned: tests/golden/ holds outputs of the reference itself
+ * (oracle/_ref/ref_harness, built from the reference sources by oracle/Makefile)
+ * and tests/test_oracle_golden.py checks this restatement against them.
+ *
+ * Every entry point takes host pointers and returns 0 or a negative
+ * MSL_ERR_* code. Floating-point expressions are evaluated one IEEE operation
+ * at a time in the functor's source order (compiled with -ffp-contract=off).
+ */
+#ifndef MSL_ORACLE_H
+#define MSL_ORACLE_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int oracle_set_threads(int n);  /* OpenMP threads for map/zip/stencil loops; returns the count in use */
+int oracle_map(int dtype, int op, const void *in, void *out, size_t n, const double *params);
+int oracle_zip(int dtype, int op, const void *a, const void *b, void *out, size_t n);
+int oracle_zip3(int dtype, int op, const void *a, const void *b, const void *c, void *out, size_t n);
+int oracle_map_index(int dtype, int op, const void *in, void *out, int ndim, const long long *dims,
+                     const double *params);
+int oracle_zip_index(int dtype, int op, const void *a, const void *b, void *out, int ndim,
+                     const long long *dims, const double *params);
+int oracle_fold(int dtype, int op, const void *in, size_t n, void *result);
+int oracle_fold_absdiff_max(int dtype, const void *a, const void *b, size_t n, double *result);
+int oracle_stencil2d(int dtype, int kind, const void *in, void *out, int rows, int cols, int radius,
+                     double neutral);
+int oracle_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, int cols, int radius,
+                             double neutral, int iters, double *residual, int *result_in_b);
+int oracle_stencil3d(int dtype, int kind, const void *in, void *out, int depth, int rows, int cols,
+                     int radius, double neutral);
+int oracle_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int rows, int cols,
+                             int radius, double neutral, int iters, double *residual, int *result_in_b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
