@@ -160,6 +160,11 @@ int msl_fold(int dtype, int op, const void *in, size_t n, void *result);
 int msl_fold_absdiff_max(int dtype, const void *a, const void *b, size_t n, double *result);
 
 /* ---- stencils ------------------------------------------------------------- */
+/* Stage stencil windows with TMA tensor copies when the grid allows it (1,
+ * the default) or always with plain coalesced loads (0). Results are
+ * identical either way; the switch exists to test and compare the loaders.
+ * No reference counterpart (the reference has no staging). */
+int msl_set_tma(int enabled);
 /* out = f(view, x, y) for every cell of a rows x cols grid; `radius` is the
  * stencil size r, `neutral` the value outside the grid. in != out.
  * DM::mapStencil<f> (src/dm.cpp:1535-1591), NPLMatrix (include/nplmatrix.h:56-168). */

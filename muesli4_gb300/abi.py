@@ -1,0 +1,256 @@
+"""ctypes binding of libmsl_gb300.so (the C ABI declared in include/msl_gb300.h).
+
+This is how Python callers -- the tests and the benchmark -- reach the GPU
+skeletons. It loads the in-tree library and raises if it is missing: there is
+no CPU fallback anywhere in the product path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "libmsl_gb300.so")
+HEADER = os.path.join(ROOT, "include", "msl_gb300.h")
+
+# Constants of msl_gb300.h (parsed from the header so they cannot drift).
+_CONST = {}
+with open(HEADER) as _f:
+    for _m in re.finditer(r"#define\s+(MSL_[A-Z0-9_]+)\s+\(?(-?\d+)\)?", _f.read()):
+        _CONST[_m.group(1)] = int(_m.group(2))
+globals().update(_CONST)
+
+NP_DTYPE = {MSL_F32: np.float32, MSL_F64: np.float64, MSL_I32: np.int32, MSL_BF16: np.uint16}  # noqa: F821
+DTYPE_OF = {np.dtype(np.float32): MSL_F32, np.dtype(np.float64): MSL_F64,  # noqa: F821
+            np.dtype(np.int32): MSL_I32, np.dtype(np.uint16): MSL_BF16}  # noqa: F821
+
+
+class MslError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+def declared_functions() -> list[str]:
+    """Names of the functions msl_gb300.h declares."""
+    with open(HEADER) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(msl_\w+)\s*\(", text, flags=re.M)))
+
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Load the in-tree libmsl_gb300.so (raises ImportError if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(LIB_PATH)
+    i, sz, d, vp = ctypes.c_int, ctypes.c_size_t, ctypes.c_double, ctypes.c_void_p
+    dp, ip, llp = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)
+    sig = {
+        "msl_init": [i], "msl_terminate": [], "msl_sync": [], "msl_get_stream": [ctypes.POINTER(vp)],
+        "msl_set_stream": [vp], "msl_device_info": [ip, ctypes.POINTER(sz), ctypes.POINTER(sz)],
+        "msl_launch_count": [ctypes.POINTER(ctypes.c_ulonglong)], "msl_set_tma": [i],
+        "msl_alloc": [ctypes.POINTER(vp), sz], "msl_free": [vp], "msl_upload": [vp, vp, sz],
+        "msl_download": [vp, vp, sz], "msl_copy": [vp, vp, sz], "msl_fill": [i, vp, sz, d],
+        "msl_map": [i, i, vp, vp, sz, dp], "msl_zip": [i, i, vp, vp, vp, sz], "msl_zip3": [i, i, vp, vp, vp, vp, sz],
+        "msl_map_index": [i, i, vp, vp, i, llp, dp], "msl_zip_index": [i, i, vp, vp, vp, i, llp, dp],
+        "msl_fold": [i, i, vp, sz, vp], "msl_fold_absdiff_max": [i, vp, vp, sz, dp],
+        "msl_stencil2d": [i, i, vp, vp, i, i, i, d], "msl_stencil2d_iterate": [i, i, vp, vp, i, i, i, d, i, dp, ip],
+        "msl_stencil3d": [i, i, vp, vp, i, i, i, i, d],
+        "msl_stencil3d_iterate": [i, i, vp, vp, i, i, i, i, d, i, dp, ip],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    L.msl_last_error_string.argtypes = []
+    L.msl_last_error_string.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc != 0:
+        msg = load().msl_last_error_string().decode(errors="replace")
+        raise MslError(rc, f"{what}: {msg}" if what else msg)
+
+
+def init(device: int = 0) -> None:
+    check(load().msl_init(device), "msl_init")
+
+
+def terminate() -> None:
+    check(load().msl_terminate(), "msl_terminate")
+
+
+def sync() -> None:
+    check(load().msl_sync(), "msl_sync")
+
+
+def stream_handle() -> int:
+    s = ctypes.c_void_p()
+    check(load().msl_get_stream(ctypes.byref(s)), "msl_get_stream")
+    return s.value or 0
+
+
+def launch_count() -> int:
+    c = ctypes.c_ulonglong()
+    check(load().msl_launch_count(ctypes.byref(c)))
+    return c.value
+
+
+def set_tma(enabled: bool) -> None:
+    check(load().msl_set_tma(1 if enabled else 0))
+
+
+def device_info():
+    sm, fr, to = ctypes.c_int(), ctypes.c_size_t(), ctypes.c_size_t()
+    check(load().msl_device_info(ctypes.byref(sm), ctypes.byref(fr), ctypes.byref(to)))
+    return sm.value, fr.value, to.value
+
+
+class DeviceArray:
+    """A device buffer owned through msl_alloc/msl_free, with a numpy shape/dtype."""
+
+    def __init__(self, shape, dtype, ptr: int | None = None):
+        self.shape = tuple(int(s) for s in (shape if isinstance(shape, (tuple, list)) else (shape,)))
+        self.dtype = np.dtype(dtype)
+        self.size = int(np.prod(self.shape)) if self.shape else 1
+        self.nbytes = self.size * self.dtype.itemsize
+        self._owned = ptr is None
+        if ptr is None:
+            p = ctypes.c_void_p()
+            check(load().msl_alloc(ctypes.byref(p), self.nbytes), "msl_alloc")
+            ptr = p.value or 0
+        self.ptr = ptr
+
+    @classmethod
+    def from_host(cls, a: np.ndarray) -> "DeviceArray":
+        a = np.ascontiguousarray(a)
+        d = cls(a.shape, a.dtype)
+        d.upload(a)
+        return d
+
+    def upload(self, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=self.dtype)
+        assert a.size == self.size
+        check(load().msl_upload(self.ptr, a.ctypes.data, self.nbytes), "msl_upload")
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.shape, self.dtype)
+        check(load().msl_download(out.ctypes.data, self.ptr, self.nbytes), "msl_download")
+        return out
+
+    @property
+    def code(self) -> int:
+        return DTYPE_OF[self.dtype]
+
+    def free(self) -> None:
+        if self._owned and self.ptr:
+            L = _lib
+            if L is not None:
+                L.msl_free(self.ptr)
+            self.ptr = 0
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _params(p):
+    if p is None:
+        return None
+    vals = [float(v) for v in p] + [0.0] * (8 - len(p))
+    return (ctypes.c_double * 8)(*vals)
+
+
+def _dims(shape):
+    return (ctypes.c_longlong * 3)(*shape, *([0] * (3 - len(shape))))
+
+
+# ---- skeleton calls on DeviceArrays -------------------------------------------------
+def fill(x: DeviceArray, value: float) -> None:
+    check(load().msl_fill(x.code, x.ptr, x.size, float(value)), "msl_fill")
+
+
+def copy(dst: DeviceArray, src: DeviceArray) -> None:
+    check(load().msl_copy(dst.ptr, src.ptr, src.nbytes), "msl_copy")
+
+
+def map(op: int, x: DeviceArray, out: DeviceArray, params=None) -> None:
+    check(load().msl_map(x.code, op, x.ptr, out.ptr, x.size, _params(params)), "msl_map")
+
+
+def zip(op: int, a: DeviceArray, b: DeviceArray, out: DeviceArray) -> None:
+    check(load().msl_zip(a.code, op, a.ptr, b.ptr, out.ptr, a.size), "msl_zip")
+
+
+def zip3(op: int, a: DeviceArray, b: DeviceArray, c: DeviceArray, out: DeviceArray) -> None:
+    check(load().msl_zip3(a.code, op, a.ptr, b.ptr, c.ptr, out.ptr, a.size), "msl_zip3")
+
+
+def map_index(op: int, x: DeviceArray, out: DeviceArray, params=None) -> None:
+    check(load().msl_map_index(x.code, op, x.ptr, out.ptr, len(x.shape), _dims(x.shape), _params(params)),
+          "msl_map_index")
+
+
+def zip_index(op: int, a: DeviceArray, b: DeviceArray, out: DeviceArray, params=None) -> None:
+    check(load().msl_zip_index(a.code, op, a.ptr, b.ptr, out.ptr, len(a.shape), _dims(a.shape), _params(params)),
+          "msl_zip_index")
+
+
+def fold(op: int, x: DeviceArray):
+    res = np.zeros(1, x.dtype)
+    check(load().msl_fold(x.code, op, x.ptr, x.size, res.ctypes.data), "msl_fold")
+    return res[0]
+
+
+def fold_absdiff_max(a: DeviceArray, b: DeviceArray) -> float:
+    r = ctypes.c_double()
+    check(load().msl_fold_absdiff_max(a.code, a.ptr, b.ptr, a.size, ctypes.byref(r)), "msl_fold_absdiff_max")
+    return r.value
+
+
+def stencil2d(kind: int, x: DeviceArray, out: DeviceArray, radius: int, neutral: float) -> None:
+    rows, cols = x.shape
+    check(load().msl_stencil2d(x.code, kind, x.ptr, out.ptr, rows, cols, radius, float(neutral)), "msl_stencil2d")
+
+
+def stencil2d_iterate(kind: int, a: DeviceArray, b: DeviceArray, radius: int, neutral: float, iters: int,
+                      residual: bool = True):
+    """Ping-pong sweeps; returns (array holding the last sweep, residual or None)."""
+    rows, cols = a.shape
+    r = ctypes.c_double()
+    inb = ctypes.c_int()
+    check(load().msl_stencil2d_iterate(a.code, kind, a.ptr, b.ptr, rows, cols, radius, float(neutral), iters,
+                                       ctypes.byref(r) if residual else None, ctypes.byref(inb)),
+          "msl_stencil2d_iterate")
+    return (b if inb.value else a), (r.value if residual else None)
+
+
+def stencil3d(kind: int, x: DeviceArray, out: DeviceArray, radius: int, neutral: float) -> None:
+    d, rows, cols = x.shape
+    check(load().msl_stencil3d(x.code, kind, x.ptr, out.ptr, d, rows, cols, radius, float(neutral)), "msl_stencil3d")
+
+
+def stencil3d_iterate(kind: int, a: DeviceArray, b: DeviceArray, radius: int, neutral: float, iters: int,
+                      residual: bool = True):
+    d, rows, cols = a.shape
+    r = ctypes.c_double()
+    inb = ctypes.c_int()
+    check(load().msl_stencil3d_iterate(a.code, kind, a.ptr, b.ptr, d, rows, cols, radius, float(neutral), iters,
+                                       ctypes.byref(r) if residual else None, ctypes.byref(inb)),
+          "msl_stencil3d_iterate")
+    return (b if inb.value else a), (r.value if residual else None)

@@ -1,0 +1,130 @@
+// Built-in stencil functors of libmsl_gb300.so (internal header).
+//
+// Reference functors: examples/heatdiffusion.cpp:55-76 (heat2D, heat3D),
+// examples/gameoflife.cpp:22-42 (Life), examples/meanblur2.cpp:46-57 (box).
+#pragma once
+
+#include "../include/detail/msl_stencil.cuh"
+#include "msl_internal.h"
+
+namespace msl {
+namespace builtin {
+
+using namespace msl::gpu;
+
+
+template <typename T> __device__ __forceinline__ T div_rn(T a, T b);
+template <> __device__ __forceinline__ float div_rn<float>(float a, float b) { return __fdiv_rn(a, b); }
+template <> __device__ __forceinline__ double div_rn<double>(double a, double b) { return __ddiv_rn(a, b); }
+
+// heat2D: (((0 + W) + E) + N) + S, then / 4 (examples/heatdiffusion.cpp:67-76).
+template <typename T, class V> __device__ __forceinline__ T heat5(const V &m, int x, int y) {
+    T v = T(0);
+    v = Arith<T>::add(v, m(x - 1, y));
+    v = Arith<T>::add(v, m(x + 1, y));
+    v = Arith<T>::add(v, m(x, y - 1));
+    v = Arith<T>::add(v, m(x, y + 1));
+    return div_rn<T>(v, T(4));
+}
+template <typename T> struct StHeat5 {
+    template <class V> __device__ __forceinline__ T operator()(const V &m, int x, int y) const { return heat5<T>(m, x, y); }
+};
+// Plain Jacobi: boundary cells keep their value, inside cells take heat2D.
+template <typename T> struct StJacobi5 {
+    template <class V> __device__ __forceinline__ T operator()(const V &m, int x, int y) const {
+        if (x == 0 || y == 0 || x == m.width - 1 || y == m.height - 1) return m(x, y);
+        return heat5<T>(m, x, y);
+    }
+};
+// Box over (2R+1)^2 cells, summed dx outer / dy inner as the meanblur loop
+// nest (examples/meanblur2.cpp:46-57). strip() computes kSt2RPT vertically
+// adjacent outputs reusing each loaded column: for every dx it loads the
+// RPT + 2R cells of that column once and adds them to the RPT sums, so each
+// output still receives its (dx, dy) terms in the reference's order.
+template <typename T, int R, bool MEAN> struct StBoxFixed {
+    static constexpr bool kStrip2 = true;  // has a strip() (detected by has_strip2)
+    template <class V> __device__ __forceinline__ T finish(T s) const {
+        return MEAN ? div_rn<T>(s, T((2 * R + 1) * (2 * R + 1))) : s;
+    }
+    template <class V> __device__ __forceinline__ T operator()(const V &m, int x, int y) const {
+        T s = T(0);
+#pragma unroll
+        for (int dx = -R; dx <= R; dx++)
+#pragma unroll
+            for (int dy = -R; dy <= R; dy++) s = Arith<T>::add(s, m(x + dx, y + dy));
+        return finish<V>(s);
+    }
+    template <class V> __device__ __forceinline__ void strip(const V &m, int x, int y0, T (&out)[kSt2RPT]) const {
+        T s[kSt2RPT];
+#pragma unroll
+        for (int j = 0; j < kSt2RPT; j++) s[j] = T(0);
+#pragma unroll 1
+        for (int dx = -R; dx <= R; dx++) {
+            T col[kSt2RPT + 2 * R];
+#pragma unroll
+            for (int k = 0; k < kSt2RPT + 2 * R; k++) col[k] = m(x + dx, y0 - R + k);
+#pragma unroll
+            for (int j = 0; j < kSt2RPT; j++)
+#pragma unroll
+                for (int dy = 0; dy <= 2 * R; dy++) s[j] = Arith<T>::add(s[j], col[j + dy]);
+        }
+#pragma unroll
+        for (int j = 0; j < kSt2RPT; j++) out[j] = finish<V>(s[j]);
+    }
+};
+// Any radius (runtime), one output at a time.
+template <typename T> struct StBoxAny {
+    int r;
+    bool mean;
+    template <class V> __device__ __forceinline__ T operator()(const V &m, int x, int y) const {
+        T s = T(0);
+        for (int dx = -r; dx <= r; dx++)
+            for (int dy = -r; dy <= r; dy++) s = Arith<T>::add(s, m(x + dx, y + dy));
+        return mean ? div_rn<T>(s, T((2 * r + 1) * (2 * r + 1))) : s;
+    }
+};
+// Conway's rule (examples/gameoflife.cpp:22-42), dead cells outside.
+struct StLife {
+    template <class V> __device__ __forceinline__ int32_t operator()(const V &m, int x, int y) const {
+        int32_t sum = m(x, y - 1) + m(x - 1, y - 1) + m(x + 1, y - 1) + m(x, y + 1) + m(x - 1, y + 1) +
+                      m(x + 1, y + 1) + m(x - 1, y) + m(x + 1, y);
+        int32_t alive = m(x, y);
+        int32_t next = 0;
+        if (alive == 1 && (sum == 2 || sum == 3)) next = 1;
+        if (alive == 0 && sum == 3) next = 1;
+        return next;
+    }
+};
+// heat3D: ((((((0 + W) + E) + N) + S) + B) + F) / 6 (examples/heatdiffusion.cpp:55-65).
+template <typename T> struct StHeat7 {
+    template <class V> __device__ __forceinline__ T operator()(const V &c, int x, int y, int z) const {
+        T v = T(0);
+        v = Arith<T>::add(v, c(x - 1, y, z));
+        v = Arith<T>::add(v, c(x + 1, y, z));
+        v = Arith<T>::add(v, c(x, y - 1, z));
+        v = Arith<T>::add(v, c(x, y + 1, z));
+        v = Arith<T>::add(v, c(x, y, z - 1));
+        v = Arith<T>::add(v, c(x, y, z + 1));
+        return div_rn<T>(v, T(6));
+    }
+};
+// 3-D box, dx outer, dy, dz inner (examples/meanblur2.cpp:46-57).
+template <typename T> struct StBox3 {
+    int r;
+    bool mean;
+    template <class V> __device__ __forceinline__ T operator()(const V &c, int x, int y, int z) const {
+        T s = T(0);
+        for (int dx = -r; dx <= r; dx++)
+            for (int dy = -r; dy <= r; dy++)
+                for (int dz = -r; dz <= r; dz++) s = Arith<T>::add(s, c(x + dx, y + dy, z + dz));
+        return mean ? div_rn<T>(s, T((2 * r + 1) * (2 * r + 1) * (2 * r + 1))) : s;
+    }
+};
+
+// Launch a fixed-radius box sweep (F32); defined in stencil_box_*.cu.
+template <int R>
+cudaError_t box_fixed_f32(const float *in, float *out, int rows, int cols, float neutral, bool mean,
+                          unsigned long long *resid, bool tma);
+
+}  // namespace builtin
+}  // namespace msl

@@ -1,0 +1,487 @@
+// Stencil skeletons: DM::mapStencil (2-D) and DC::mapStencil (3-D).
+//
+// Reference (include/detail/map_kernels.cuh:140-168, src/dm.cpp:1535-1591,
+// src/dc.cpp:559-592): one thread per cell in a 1-D grid; every neighbour
+// read goes through NPLMatrix/PLCube::operator(), a branchy bounds check plus
+// a global load (include/nplmatrix.h:123-139, include/plcube.h:105-119).
+//
+// Here the halo handling becomes a tile staged in shared memory:
+//  * 2-D: each CTA owns a 64 x 32 block of outputs; one TMA 2-D load
+//    (cp.async.bulk.tensor.2d, completion on an mbarrier) brings the block
+//    plus its halo into shared memory; each thread evaluates the functor for a
+//    vertical strip of 8 cells of one column (a warp covers 32 consecutive
+//    columns, so shared-memory reads are conflict-free and global stores are
+//    coalesced).
+//  * 3-D: each CTA owns a 64 x 16 column of the cube for a chunk of planes and
+//    marches along z with a ring of shared-memory planes (2r+1 in use, one in
+//    flight), one TMA 3-D load per plane.
+// The functor sees the same view type the reference passes (NPLMatrix /
+// PLCube): public width/height[/depth], neutralValue, stencilSize and
+// operator()(x, y[, z]) that returns neutralValue outside the grid. Reads that
+// hit the staged window come from shared memory; any other read (a functor
+// reaching beyond the radius it declared) falls through to global memory, so
+// the semantics are the reference's for every functor. Tiles whose staged
+// window lies inside the grid run the functor with the bounds test compiled
+// out. Where TMA cannot address the grid (row pitch not a multiple of 16
+// bytes, misaligned base, oversized halo) the same kernel stages the window
+// with plain coalesced loads.
+//
+// Optional fused residual: max |new - old| over the sweep, in FP64, reduced in
+// the CTA and folded into one device word with an atomic max (non-negative
+// doubles order like their bit patterns).
+#pragma once
+
+#include <cuda.h>
+
+#include <type_traits>
+
+#include "msl_device.cuh"
+
+namespace msl {
+
+// ---- views (the types user stencil functors receive) ---------------------------
+// T is the arithmetic type the functor sees, S the storage type (S == T except
+// for bfloat16 storage, where T is float).
+template <typename T, typename S = T> class NPLMatrix {
+   public:
+    int width = 0, height = 0;
+    int stencilSize = 0;
+    T neutralValue{};
+    // staging window: tile_[ty * pitch_ + tx] holds cell (ox_ + tx, oy_ + ty)
+    const S *tile_ = nullptr;
+    const S *global_ = nullptr;
+    int ox_ = 0, oy_ = 0, pitch_ = 0, tile_h_ = 0;
+    bool check_ = true;
+
+    __device__ __forceinline__ T operator()(int x, int y) const {
+        const unsigned tx = (unsigned)(x - ox_), ty = (unsigned)(y - oy_);
+        if (tx < (unsigned)pitch_ && ty < (unsigned)tile_h_) {
+            if (!check_ || ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height))
+                return gpu::widen<S>(tile_[ty * pitch_ + tx]);
+            return neutralValue;
+        }
+        if ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height)
+            return gpu::widen<S>(global_[(size_t)y * width + x]);
+        return neutralValue;
+    }
+};
+
+template <typename T, typename S = T> class PLCube {
+   public:
+    int width = 0, height = 0, depth = 0;
+    int stencilSize = 0;
+    T neutralValue{};
+    // ring of planes: plane z lives in slot (z & mask_) while zlo_ <= z <= zhi_
+    const S *ring_ = nullptr;
+    const S *global_ = nullptr;
+    int ox_ = 0, oy_ = 0, pitch_ = 0, tile_h_ = 0, plane_ = 0, mask_ = 0, zlo_ = 0, zhi_ = -1;
+    bool check_ = true;
+
+    __device__ __forceinline__ T operator()(int x, int y, int z) const {
+        const unsigned tx = (unsigned)(x - ox_), ty = (unsigned)(y - oy_);
+        if (tx < (unsigned)pitch_ && ty < (unsigned)tile_h_ && z >= zlo_ && z <= zhi_) {
+            if (!check_ || ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height &&
+                            (unsigned)z < (unsigned)depth))
+                return gpu::widen<S>(ring_[(z & mask_) * plane_ + ty * pitch_ + tx]);
+            return neutralValue;
+        }
+        if ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height && (unsigned)z < (unsigned)depth)
+            return gpu::widen<S>(global_[((size_t)z * height + y) * width + x]);
+        return neutralValue;
+    }
+};
+
+namespace gpu {
+
+constexpr int kSt2BX = 64, kSt2BY = 32, kSt2RPT = 8, kSt2Threads = 256;
+constexpr int kSt3BX = 64, kSt3BY = 16, kSt3RPT = 4, kSt3Threads = 256;
+constexpr int kStHeader = 128;  // mbarriers live in the first 128 bytes of dynamic smem
+
+// Halo in x, rounded up to 16 bytes so that a TMA box starting at x0 - hx keeps
+// its innermost coordinate 16-byte aligned (x0 is a multiple of 64).
+template <typename S> MSL_HD int halo_x(int r) {
+    const int q = (int)(16 / sizeof(S));
+    return (r + q - 1) / q * q;
+}
+
+// Functors may provide strip(view, x, y0, vals) computing kSt2RPT vertically
+// adjacent cells at once (register reuse); others are called per cell.
+template <class F, class = void> struct has_strip2 : std::false_type {};
+template <class F> struct has_strip2<F, decltype((void)F::kStrip2, void())> : std::true_type {};
+
+MSL_DEV void atomic_max_nonneg(unsigned long long *slot, double v) {
+    atomicMax(slot, (unsigned long long)__double_as_longlong(v));
+}
+MSL_DEV double block_max(double v) {
+    __shared__ double s[32];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        double o = __shfl_down_sync(0xffffffffu, v, d);
+        v = (o > v || o != o) ? o : v;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s[warp] = v;
+    __syncthreads();
+    v = 0.0;
+    if (warp == 0) {
+        if (lane < (int)(blockDim.x >> 5)) v = s[lane];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            double o = __shfl_down_sync(0xffffffffu, v, d);
+            v = (o > v || o != o) ? o : v;
+        }
+    }
+    return v;
+}
+template <typename S> MSL_DEV double stored_f64(S s) { return (double)s; }
+template <> MSL_DEV double stored_f64<bf16s>(bf16s s) { return (double)bf16_to_f(s); }
+
+template <typename S, class Fn, class View>
+MSL_DEV void stencil2d_strip(const Fn &fn, const View &m, int x, int ys, int rows, int cols, S *out, bool want,
+                             double &dmax) {
+    using T = typename Compute<S>::type;
+    if (x >= cols) return;
+    if constexpr (has_strip2<Fn>::value) {
+        T vals[kSt2RPT];
+        fn.strip(m, x, ys, vals);
+#pragma unroll
+        for (int j = 0; j < kSt2RPT; j++) {
+            const int y = ys + j;
+            if (y < rows) {
+                const S sv = narrow<S>(vals[j]);
+                out[(size_t)y * cols + x] = sv;
+                if (want) {
+                    const double d = fabs(stored_f64(sv) - (double)m(x, y));
+                    if (d > dmax || d != d) dmax = d;
+                }
+            }
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < kSt2RPT; j++) {
+            const int y = ys + j;
+            if (y < rows) {
+                const S sv = narrow<S>(fn(m, x, y));
+                out[(size_t)y * cols + x] = sv;
+                if (want) {
+                    const double d = fabs(stored_f64(sv) - (double)m(x, y));
+                    if (d > dmax || d != d) dmax = d;
+                }
+            }
+        }
+    }
+}
+
+// One CTA = one 64 x 32 output block. Dynamic smem: [0,128) mbarrier, then the
+// (32 + 2r) x (64 + 2hx) window.
+template <typename S, class Fn, bool TMA>
+__global__ void __launch_bounds__(kSt2Threads)
+    stencil2d_kernel(const __grid_constant__ CUtensorMap tmap, const S *in, S *out, int rows, int cols, int r,
+                     int hx, typename Compute<S>::type neutral, Fn fn, unsigned long long *resid,
+                     unsigned *err) {
+    using T = typename Compute<S>::type;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
+    S *tile = reinterpret_cast<S *>(smem_raw + kStHeader);
+    const int pitch = kSt2BX + 2 * hx, th = kSt2BY + 2 * r;
+    const int x0 = blockIdx.x * kSt2BX, y0 = blockIdx.y * kSt2BY;
+    const int wx0 = x0 - hx, wy0 = y0 - r;
+    bool ok = true;
+    if constexpr (TMA) {
+        if (threadIdx.x == 0) {
+            mbar_init(bar, 1);
+            fence_barrier_init();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_arrive_expect_tx(bar, (uint32_t)(pitch * th * sizeof(S)));
+            tma_load_2d(tile, &tmap, bar, wx0, wy0);
+        }
+        ok = mbar_wait_bounded(bar, 0, err);
+    } else {
+        for (int i = threadIdx.x; i < pitch * th; i += blockDim.x) {
+            const int ty = i / pitch, tx = i - ty * pitch;
+            const int gx = wx0 + tx, gy = wy0 + ty;
+            tile[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows) ? in[(size_t)gy * cols + gx] : S{};
+        }
+    }
+    ok = __syncthreads_and(ok);
+    if (!ok) return;
+
+    NPLMatrix<T, S> m;
+    m.width = cols;
+    m.height = rows;
+    m.stencilSize = r;
+    m.neutralValue = neutral;
+    m.tile_ = tile;
+    m.global_ = in;
+    m.ox_ = wx0;
+    m.oy_ = wy0;
+    m.pitch_ = pitch;
+    m.tile_h_ = th;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x = x0 + (warp % (kSt2BX / 32)) * 32 + lane;
+    const int ys = y0 + (warp / (kSt2BX / 32)) * kSt2RPT;
+    const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 + pitch <= cols && wy0 + th <= rows;
+    const bool want = resid != nullptr;
+    double dmax = 0.0;
+    if (interior) {
+        m.check_ = false;
+        stencil2d_strip<S>(fn, m, x, ys, rows, cols, out, want, dmax);
+    } else {
+        m.check_ = true;
+        stencil2d_strip<S>(fn, m, x, ys, rows, cols, out, want, dmax);
+    }
+    if (want) {
+        dmax = block_max(dmax);
+        if (threadIdx.x == 0) atomic_max_nonneg(resid, dmax);
+    }
+}
+
+// One CTA = one 64 x 16 column over planes [z_begin, z_end) of its chunk.
+// Ring of NS = 2^k >= 2r+2 plane slots, one mbarrier per slot.
+template <typename S, class Fn, bool TMA>
+__global__ void __launch_bounds__(kSt3Threads)
+    stencil3d_kernel(const __grid_constant__ CUtensorMap tmap, const S *in, S *out, int depth, int rows, int cols,
+                     int r, int hx, int ns_log2, int zchunk, typename Compute<S>::type neutral, Fn fn,
+                     unsigned long long *resid, unsigned *err) {
+    using T = typename Compute<S>::type;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw);  // up to 16 slots
+    S *ring = reinterpret_cast<S *>(smem_raw + kStHeader);
+    const int NS = 1 << ns_log2, mask = NS - 1;
+    const int pitch = kSt3BX + 2 * hx, th = kSt3BY + 2 * r;
+    const int plane = (pitch * th + 31) / 32 * 32;  // keeps every slot 128-byte aligned
+    const int x0 = blockIdx.x * kSt3BX, y0 = blockIdx.y * kSt3BY;
+    const int wx0 = x0 - hx, wy0 = y0 - r;
+    const int zb = blockIdx.z * zchunk;
+    const int ze = min(depth, zb + zchunk);
+    if (zb >= ze) return;
+    const int pfirst = zb - r;  // planes pfirst .. ze-1+r are loaded, in order
+    const uint32_t plane_bytes = (uint32_t)(pitch * th * sizeof(S));
+
+    auto slot_of = [&](int p) { return p & mask; };
+    auto parity_of = [&](int p) { return (uint32_t)(((p - pfirst) >> ns_log2) & 1); };
+    auto issue = [&](int p) {  // thread 0 only (TMA) / all threads (plain loads)
+        S *dst = ring + slot_of(p) * plane;
+        if constexpr (TMA) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bars[slot_of(p)], plane_bytes);
+            tma_load_3d(dst, &tmap, &bars[slot_of(p)], wx0, wy0, p);
+        } else {
+            for (int i = threadIdx.x; i < pitch * th; i += blockDim.x) {
+                const int ty = i / pitch, tx = i - ty * pitch;
+                const int gx = wx0 + tx, gy = wy0 + ty;
+                dst[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows && p >= 0 && p < depth)
+                             ? in[((size_t)p * rows + gy) * cols + gx]
+                             : S{};
+            }
+        }
+    };
+
+    bool ok = true;
+    if constexpr (TMA) {
+        if (threadIdx.x == 0) {
+            for (int s = 0; s < NS; s++) mbar_init(&bars[s], 1);
+            fence_barrier_init();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int p = pfirst; p <= zb + r; p++) issue(p);  // planes zb-r .. zb+r (2r+1 distinct slots)
+        for (int p = pfirst; p < zb + r && ok; p++) ok = mbar_wait_bounded(&bars[slot_of(p)], parity_of(p), err);
+    } else {
+        for (int p = pfirst; p < zb + r; p++) issue(p);
+    }
+
+    PLCube<T, S> c;
+    c.width = cols;
+    c.height = rows;
+    c.depth = depth;
+    c.stencilSize = r;
+    c.neutralValue = neutral;
+    c.ring_ = ring;
+    c.global_ = in;
+    c.ox_ = wx0;
+    c.oy_ = wy0;
+    c.pitch_ = pitch;
+    c.tile_h_ = th;
+    c.plane_ = plane;
+    c.mask_ = mask;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x = x0 + (warp % (kSt3BX / 32)) * 32 + lane;
+    const int ys = y0 + (warp / (kSt3BX / 32)) * kSt3RPT;
+    const bool xy_inside = wx0 >= 0 && wy0 >= 0 && wx0 + pitch <= cols && wy0 + th <= rows;
+    const bool want = resid != nullptr;
+    double dmax = 0.0;
+
+    for (int z = zb; z < ze; z++) {
+        __syncthreads();  // every thread is done with plane z-r-1's slot
+        const int pn = z + r;      // newest plane output z needs
+        const int pf = z + r + 1;  // plane to prefetch (reuses the slot of z-r-1)
+        if constexpr (TMA) {
+            if (threadIdx.x == 0 && pf <= ze - 1 + r) issue(pf);
+            ok = ok && mbar_wait_bounded(&bars[slot_of(pn)], parity_of(pn), err);
+        } else {
+            issue(pn);
+            __syncthreads();
+        }
+        if (!__syncthreads_and(ok)) return;
+        c.zlo_ = z - r;
+        c.zhi_ = z + r;
+        const bool inside = xy_inside && z - r >= 0 && z + r < depth;
+        if (x < cols) {
+            c.check_ = true;
+#pragma unroll
+            for (int j = 0; j < kSt3RPT; j++) {
+                const int y = ys + j;
+                if (y < rows) {
+                    S sv;
+                    if (inside) {
+                        PLCube<T, S> ci = c;
+                        ci.check_ = false;
+                        sv = narrow<S>(fn(ci, x, y, z));
+                    } else {
+                        sv = narrow<S>(fn(c, x, y, z));
+                    }
+                    out[((size_t)z * rows + y) * cols + x] = sv;
+                    if (want) {
+                        const double d = fabs(stored_f64(sv) - (double)c(x, y, z));
+                        if (d > dmax || d != d) dmax = d;
+                    }
+                }
+            }
+        }
+    }
+    if (want) {
+        __syncthreads();
+        dmax = block_max(dmax);
+        if (threadIdx.x == 0) atomic_max_nonneg(resid, dmax);
+    }
+}
+
+// ---- host side --------------------------------------------------------------------
+using TensorMapEncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                        const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                                        CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                        CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
+inline TensorMapEncodeFn tensor_map_encoder() {
+    static TensorMapEncodeFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<TensorMapEncodeFn>(p);
+    }();
+    return fn;
+}
+
+template <typename S> constexpr CUtensorMapDataType tmap_dtype() {
+    if constexpr (sizeof(S) == 8) return CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    else if constexpr (sizeof(S) == 2) return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    else return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;  // 4-byte elements (float and int32 move alike)
+}
+
+inline int st3_ns_log2(int r) {
+    int ns = 1, l = 0;
+    while (ns < 2 * r + 2) ns <<= 1, l++;
+    return l;
+}
+template <typename S> inline size_t stencil2d_smem(int r) {
+    return (size_t)kStHeader + (size_t)(kSt2BX + 2 * halo_x<S>(r)) * (kSt2BY + 2 * r) * sizeof(S);
+}
+template <typename S> inline size_t stencil3d_smem(int r) {
+    const int pitch = kSt3BX + 2 * halo_x<S>(r), th = kSt3BY + 2 * r;
+    const size_t plane = (size_t)(pitch * th + 31) / 32 * 32;
+    return (size_t)kStHeader + ((size_t)1 << st3_ns_log2(r)) * plane * sizeof(S);
+}
+constexpr size_t kMaxStencilSmem = 227 * 1024;
+
+// Whether the TMA path can address this grid: 16-byte aligned base and row
+// pitch, box dimensions <= 256.
+template <typename S> inline bool stencil_tma_ok(const void *in, long long cols, int pitch, int th) {
+    return tensor_map_encoder() != nullptr && ((uintptr_t)in % 16) == 0 && (cols * (long long)sizeof(S)) % 16 == 0 &&
+           pitch <= 256 && th <= 256;
+}
+
+template <typename S, class Fn>
+cudaError_t launch_stencil2d(const S *in, S *out, int rows, int cols, int r, typename Compute<S>::type neutral,
+                             Fn fn, unsigned long long *resid, unsigned *err, cudaStream_t st, bool allow_tma = true) {
+    const int hx = halo_x<S>(r);
+    const int pitch = kSt2BX + 2 * hx, th = kSt2BY + 2 * r;
+    const size_t smem = stencil2d_smem<S>(r);
+    if (smem > kMaxStencilSmem) return cudaErrorInvalidValue;
+    dim3 grid((cols + kSt2BX - 1) / kSt2BX, (rows + kSt2BY - 1) / kSt2BY);
+    CUtensorMap map{};
+    const bool tma = allow_tma && stencil_tma_ok<S>(in, cols, pitch, th);
+    if (tma) {
+        cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+        cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(S)};
+        cuuint32_t box[2] = {(cuuint32_t)pitch, (cuuint32_t)th};
+        cuuint32_t estr[2] = {1, 1};
+        if (tensor_map_encoder()(&map, tmap_dtype<S>(), 2, const_cast<S *>(in), dims, strides, box, estr,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+        auto k = stencil2d_kernel<S, Fn, true>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, kSt2Threads, smem, st>>>(map, in, out, rows, cols, r, hx, neutral, fn, resid, err);
+    } else {
+        auto k = stencil2d_kernel<S, Fn, false>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, kSt2Threads, smem, st>>>(map, in, out, rows, cols, r, hx, neutral, fn, resid, err);
+    }
+    return cudaGetLastError();
+}
+
+template <typename S, class Fn>
+cudaError_t launch_stencil3d(const S *in, S *out, int depth, int rows, int cols, int r,
+                             typename Compute<S>::type neutral, Fn fn, unsigned long long *resid, unsigned *err,
+                             cudaStream_t st, int sm_count, bool allow_tma = true) {
+    const int hx = halo_x<S>(r);
+    const int pitch = kSt3BX + 2 * hx, th = kSt3BY + 2 * r;
+    const int ns_log2 = st3_ns_log2(r);
+    if ((1 << ns_log2) > kStHeader / 8) return cudaErrorInvalidValue;  // mbarrier slots
+    const size_t smem = stencil3d_smem<S>(r);
+    if (smem > kMaxStencilSmem) return cudaErrorInvalidValue;
+    const long long tiles = (long long)((cols + kSt3BX - 1) / kSt3BX) * ((rows + kSt3BY - 1) / kSt3BY);
+    // Enough CTAs for ~6 per SM, with chunks long enough that the 2r extra
+    // planes per chunk stay a small overhead.
+    long long target = (long long)(sm_count > 0 ? sm_count : 152) * 6;
+    long long nchunks = (target + tiles - 1) / tiles;
+    long long min_len = 8LL * (2 * r + 1);
+    long long max_chunks = (depth + min_len - 1) / min_len;
+    if (nchunks > max_chunks) nchunks = max_chunks;
+    if (nchunks < 1) nchunks = 1;
+    const int zchunk = (int)((depth + nchunks - 1) / nchunks);
+    nchunks = (depth + zchunk - 1) / zchunk;
+    dim3 grid((cols + kSt3BX - 1) / kSt3BX, (rows + kSt3BY - 1) / kSt3BY, (unsigned)nchunks);
+    CUtensorMap map{};
+    const bool tma = allow_tma && stencil_tma_ok<S>(in, cols, pitch, th);
+    if (tma) {
+        cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)depth};
+        cuuint64_t strides[2] = {(cuuint64_t)cols * sizeof(S), (cuuint64_t)cols * rows * sizeof(S)};
+        cuuint32_t box[3] = {(cuuint32_t)pitch, (cuuint32_t)th, 1};
+        cuuint32_t estr[3] = {1, 1, 1};
+        if (tensor_map_encoder()(&map, tmap_dtype<S>(), 3, const_cast<S *>(in), dims, strides, box, estr,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+        auto k = stencil3d_kernel<S, Fn, true>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, kSt3Threads, smem, st>>>(map, in, out, depth, rows, cols, r, hx, ns_log2, zchunk, neutral, fn,
+                                            resid, err);
+    } else {
+        auto k = stencil3d_kernel<S, Fn, false>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, kSt3Threads, smem, st>>>(map, in, out, depth, rows, cols, r, hx, ns_log2, zchunk, neutral, fn,
+                                            resid, err);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace gpu
+}  // namespace msl

@@ -1,0 +1,52 @@
+"""C-ABI checks that need no GPU: the library builds for sm_103a, loads, and
+exports every function include/msl_gb300.h declares; calls before msl_init
+fail with a status code instead of crashing or exiting."""
+import ctypes
+
+import pytest
+
+from muesli4_gb300 import abi, build
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return abi.load()
+
+
+def test_header_declares_the_hot_path(lib):
+    names = abi.declared_functions()
+    for required in ("msl_init", "msl_map", "msl_zip", "msl_zip3", "msl_map_index", "msl_zip_index", "msl_fold",
+                     "msl_fold_absdiff_max", "msl_copy", "msl_download", "msl_stencil2d", "msl_stencil2d_iterate",
+                     "msl_stencil3d", "msl_stencil3d_iterate"):
+        assert required in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    missing = [n for n in abi.declared_functions() if not hasattr(lib, n)]
+    assert not missing
+
+
+def test_calls_before_init_report_not_initialized(lib):
+    p = ctypes.c_void_p()
+    assert lib.msl_alloc(ctypes.byref(p), 16) == abi.MSL_ERR_NOT_INITIALIZED
+    assert b"msl_init" in lib.msl_last_error_string()
+    assert lib.msl_map(abi.MSL_F32, abi.MSL_MAP_AFFINE, None, None, 4, None) == abi.MSL_ERR_NOT_INITIALIZED
+    assert lib.msl_fold(abi.MSL_F32, abi.MSL_FOLD_SUM, None, 4, None) == abi.MSL_ERR_NOT_INITIALIZED
+    assert lib.msl_terminate() == abi.MSL_OK  # terminating an idle library is a no-op
+    c = ctypes.c_ulonglong()
+    assert lib.msl_launch_count(ctypes.byref(c)) == abi.MSL_OK
+
+
+def test_init_without_a_device_fails_cleanly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    rc = lib.msl_init(0)
+    assert rc in (abi.MSL_ERR_CUDA, abi.MSL_ERR_INVALID_ARGUMENT)
+    assert lib.msl_last_error_string()
+
+
+def test_status_codes_are_distinct():
+    codes = [v for k, v in vars(abi).items() if k.startswith("MSL_ERR_")]
+    assert len(codes) == len(set(codes)) and all(c < 0 for c in codes)
