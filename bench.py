@@ -1,0 +1,641 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 skeleton hot path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+
+Workloads (seeded synthetic inputs; shapes and value distributions of the
+reference's examples):
+  stencil_suite (default) -- the radius sweep and 3-D stencils: DM<float>
+      8192^2 box mean at r = 1, 2, 4, 6, 8, 10 (one sweep each), DM<int> 8192^2
+      Game of Life (200 steps), DC<float> 512^3 heat3D (100 steps). One step is
+      one pass over all three parts. Metric: stencil GCUPS (cell updates / s).
+  jacobi -- plain 2-D Jacobi, DM<float> 1024^2, 100 sweeps + FP64 residual.
+  mapzipfold -- DA<float> 2^28 map/zip/fold(+) and DA<int> 2^28 mapIndex/fold(+).
+      Metric: GB/s of algorithmic traffic.
+  box / life / heat -- one part of the suite alone.
+
+Prints one JSON line (rank 0). `value` is measured with device-resident inputs
+(CUDA events on the library stream around K steps, max over ranks); `e2e` is
+the same metric through the C ABI with host buffers, the host->device copy of
+every step's inputs and the device->host copy of its results inside the timed
+region. `roofline` is the dominant kernel's algorithmic bytes per launch over
+its average launch time (events on the same stream) against the measured HBM
+copy bandwidth. `cpu_baseline` is the CPU oracle (a restatement of the
+reference's OpenMP loops) timed on a bounded sample on this host's cores.
+--impl reference times that CPU implementation alone on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+# ---- distributed plumbing (replicas only: no data-path collective) ------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---- clocks sampled during the timed region ------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---- timing helpers on the library stream -------------------------------------------
+class Events:
+    """CUDA events recorded on libmsl_gb300's stream (via torch's external-stream view)."""
+
+    def __init__(self, abi):
+        import torch
+        self.torch = torch
+        self.stream = torch.cuda.ExternalStream(abi.stream_handle())
+
+    def record(self):
+        e = self.torch.cuda.Event(enable_timing=True)
+        e.record(self.stream)
+        return e
+
+    @staticmethod
+    def ms(a, b) -> float:
+        return a.elapsed_time(b)
+
+
+def pinned(shape, dtype):
+    import torch
+    tdt = {np.dtype(np.float32): torch.float32, np.dtype(np.int32): torch.int32,
+           np.dtype(np.float64): torch.float64, np.dtype(np.uint16): torch.int16}[np.dtype(dtype)]
+    t = torch.empty(shape, dtype=tdt, pin_memory=True)
+    return t, t.numpy().view(dtype)
+
+
+# ---- workloads ------------------------------------------------------------------------
+BOX_RADII = (1, 2, 4, 6, 8, 10)
+
+
+class Part:
+    """One stencil part of a workload: device buffers, host mirrors, step and oracle sample."""
+
+    def __init__(self, name, updates, launches, bytes_per_launch, dtype):
+        self.name, self.updates, self.launches = name, updates, launches
+        self.bytes_per_launch, self.dtype = bytes_per_launch, dtype
+        self.ms = 0.0
+
+
+class StencilSuite:
+    name = "stencil_suite"
+    metric = "stencil GCUPS"
+    unit = "GCUPS"
+    dtype = "f32+i32"
+
+    def __init__(self, abi, parts=("box", "life", "heat"), life_steps=200, heat_steps=100, side=8192, cube=512):
+        self.A = abi
+        self.which = parts
+        self.life_steps, self.heat_steps, self.side, self.cube = life_steps, heat_steps, side, cube
+        self.parts = {}
+        n2, n3 = side * side, cube ** 3
+        if "box" in parts:
+            self.parts["box"] = Part("box_mean_r1-10", n2 * len(BOX_RADII), len(BOX_RADII), 8 * n2, "f32")
+        if "life" in parts:
+            self.parts["life"] = Part("life", n2 * life_steps, life_steps, 8 * n2, "i32")
+        if "heat" in parts:
+            self.parts["heat"] = Part("heat3d", n3 * heat_steps, heat_steps, 8 * n3, "f32")
+
+    def config(self):
+        c = {"workload": "stencil radius sweep + 3-D stencils (" + "+".join(p.name for p in self.parts.values()) + ")",
+             "l2": "inputs larger than L2 (every grid >= 256 MiB)"}
+        if "box" in self.parts:
+            c["box"] = f"DM<float> {self.side}^2, U[0,255], mean over (2r+1)^2, r in {list(BOX_RADII)}, 1 sweep each"
+        if "life" in self.parts:
+            c["life"] = f"DM<int> {self.side}^2, Bernoulli(0.3), {self.life_steps} steps, dead border"
+        if "heat" in self.parts:
+            c["heat"] = f"DC<float> {self.cube}^3, U[0,1), 7-point heat3D, {self.heat_steps} steps, Dirichlet 0"
+        return c
+
+    def setup(self):
+        from muesli4_gb300 import workloads as W
+        A = self.A
+        s, m = self.side, self.cube
+        self.host_in, self.host_out, self.dev = {}, {}, {}
+        if "box" in self.parts:
+            img = W.blur_image(s, s, 42)
+            t, h = pinned(img.shape, np.float32)
+            h[...] = img
+            self.host_in["box"] = (t, h)
+            self.host_out["box"] = pinned(img.shape, np.float32)
+            self.dev["box"] = (A.DeviceArray.from_host(img), A.DeviceArray(img.shape, np.float32))
+        if "life" in self.parts:
+            board = W.life_board(s, s, 42)
+            t, h = pinned(board.shape, np.int32)
+            h[...] = board
+            self.host_in["life"] = (t, h)
+            self.host_out["life"] = pinned(board.shape, np.int32)
+            self.dev["life"] = [A.DeviceArray.from_host(board), A.DeviceArray(board.shape, np.int32)]
+        if "heat" in self.parts:
+            cube = W.heat_cube(m, m, m, 42)
+            t, h = pinned(cube.shape, np.float32)
+            h[...] = cube
+            self.host_in["heat"] = (t, h)
+            self.host_out["heat"] = pinned(cube.shape, np.float32)
+            self.dev["heat"] = [A.DeviceArray.from_host(cube), A.DeviceArray(cube.shape, np.float32)]
+        self.h2d = sum(h.nbytes for _, h in self.host_in.values())
+        self.d2h = sum(h.nbytes for _, h in self.host_out.values())
+
+    def updates(self):
+        return sum(p.updates for p in self.parts.values())
+
+    def step(self, ev=None, marks=None):
+        """One pass over the parts on the device. With `ev`, records an event
+        after each part into `marks`."""
+        A = self.A
+        if "box" in self.parts:
+            src, dst = self.dev["box"]
+            for r in BOX_RADII:
+                A.stencil2d(A.MSL_ST2_BOXMEAN, src, dst, r, 0.0)
+            if ev is not None:
+                marks.append(("box", ev.record()))
+        if "life" in self.parts:
+            a, b = self.dev["life"]
+            last, _ = A.stencil2d_iterate(A.MSL_ST2_LIFE, a, b, 1, 0, self.life_steps, residual=False)
+            if last is b:
+                self.dev["life"] = [b, a]
+            if ev is not None:
+                marks.append(("life", ev.record()))
+        if "heat" in self.parts:
+            a, b = self.dev["heat"]
+            last, _ = A.stencil3d_iterate(A.MSL_ST3_HEAT7, a, b, 1, 0.0, self.heat_steps, residual=False)
+            if last is b:
+                self.dev["heat"] = [b, a]
+            if ev is not None:
+                marks.append(("heat", ev.record()))
+
+    def e2e_step(self):
+        """Host buffers in, host buffers out, through the C ABI."""
+        A = self.A
+        for k, (_, h) in self.host_in.items():
+            d = self.dev[k][0]
+            A.check(A.load().msl_upload(d.ptr, h.ctypes.data, h.nbytes), "msl_upload")
+        self.step()
+        for k, (_, h) in self.host_out.items():
+            d = self.dev[k][1] if k == "box" else self.dev[k][0]
+            A.check(A.load().msl_download(h.ctypes.data, d.ptr, h.nbytes), "msl_download")
+
+    # CPU sample: per-part rates measured on bounded samples, combined in the
+    # workload's own mix of cell updates.
+    def cpu_sample(self, O, threads, min_seconds: float = 0.0):
+        """Per-part CPU rates on bounded samples (repeated until min_seconds),
+        combined in this workload's own mix of cell updates."""
+        from muesli4_gb300 import workloads as W
+        O.set_threads(threads)
+        done = {k: 0.0 for k in self.parts}
+        spent = {k: 0.0 for k in self.parts}
+        desc = []
+        img = W.blur_image(512, self.side, 42) if "box" in self.parts else None
+        board = W.life_board(2048, self.side, 42) if "life" in self.parts else None
+        cube = W.heat_cube(64, self.cube, self.cube, 42) if "heat" in self.parts else None
+        if img is not None:
+            desc.append(f"box r=1..10 on {img.shape[0]}x{self.side}")
+        if board is not None:
+            desc.append(f"life 4 steps on {board.shape[0]}x{self.side}")
+        if cube is not None:
+            desc.append(f"heat3d 4 steps on {cube.shape[0]}x{self.cube}x{self.cube}")
+        t_begin = time.perf_counter()
+        while True:
+            if img is not None:
+                for r in BOX_RADII:
+                    t0 = time.perf_counter()
+                    O.stencil2d(2, img, r, 0.0)
+                    spent["box"] += time.perf_counter() - t0
+                done["box"] += img.size * len(BOX_RADII)
+            if board is not None:
+                t0 = time.perf_counter()
+                O.stencil2d_iterate(4, board, 1, 0, 4)
+                spent["life"] += time.perf_counter() - t0
+                done["life"] += 4 * board.size
+            if cube is not None:
+                t0 = time.perf_counter()
+                O.stencil3d_iterate(0, cube, 1, 0.0, 4)
+                spent["heat"] += time.perf_counter() - t0
+                done["heat"] += 4 * cube.size
+            if time.perf_counter() - t_begin >= min_seconds:
+                break
+        total_t = sum(self.parts[k].updates * spent[k] / done[k] for k in self.parts)
+        return self.updates() / total_t / 1e9, "; ".join(desc) + f" ({time.perf_counter() - t_begin:.1f} s)"
+
+
+class Jacobi:
+    name = "jacobi"
+    metric = "stencil GCUPS"
+    unit = "GCUPS"
+    dtype = "f32"
+
+    def __init__(self, abi, side=1024, iters=100):
+        self.A, self.side, self.iters = abi, side, iters
+        self.parts = {"jacobi": Part("jacobi5", side * side * iters, iters, 8 * side * side, "f32")}
+
+    def config(self):
+        return {"workload": f"plain Jacobi DM<float> {self.side}^2, 5-point, {self.iters} sweeps + FP64 residual",
+                "l2": "grid (8 MiB) is L2-resident: the HBM fraction is effective bandwidth"}
+
+    def setup(self):
+        from muesli4_gb300 import workloads as W
+        A = self.A
+        g = W.jacobi_grid(self.side, self.side, 42)
+        t, h = pinned(g.shape, np.float32)
+        h[...] = g
+        self.host_in = {"jacobi": (t, h)}
+        self.host_out = {"jacobi": pinned(g.shape, np.float32)}
+        self.dev = {"jacobi": [A.DeviceArray.from_host(g), A.DeviceArray(g.shape, np.float32)]}
+        self.h2d, self.d2h = h.nbytes, h.nbytes + 8
+        self.residual = None
+
+    def updates(self):
+        return self.parts["jacobi"].updates
+
+    def step(self, ev=None, marks=None):
+        A = self.A
+        a, b = self.dev["jacobi"]
+        last, self.residual = A.stencil2d_iterate(A.MSL_ST2_JACOBI5, a, b, 1, 0.0, self.iters, residual=True)
+        if ev is not None:
+            marks.append(("jacobi", ev.record()))
+
+    def e2e_step(self):
+        A = self.A
+        _, h = self.host_in["jacobi"]
+        a, b = self.dev["jacobi"]
+        A.check(A.load().msl_upload(a.ptr, h.ctypes.data, h.nbytes), "msl_upload")
+        last, self.residual = A.stencil2d_iterate(A.MSL_ST2_JACOBI5, a, b, 1, 0.0, self.iters, residual=True)
+        _, ho = self.host_out["jacobi"]
+        A.check(A.load().msl_download(ho.ctypes.data, last.ptr, ho.nbytes), "msl_download")
+
+    def cpu_sample(self, O, threads, min_seconds: float = 0.0):
+        from muesli4_gb300 import workloads as W
+        O.set_threads(threads)
+        g = W.jacobi_grid(self.side, self.side, 42)
+        t0 = time.perf_counter()
+        O.stencil2d_iterate(0, g, 1, 0.0, 20)
+        return 20 * self.side * self.side / (time.perf_counter() - t0) / 1e9, f"20 sweeps on {self.side}^2"
+
+
+class MapZipFold:
+    name = "mapzipfold"
+    metric = "map/zip/fold GB/s"
+    unit = "GB/s"
+    dtype = "f32+i32"
+
+    def __init__(self, abi, n=1 << 28):
+        self.A, self.n = abi, n
+        b = 4 * n
+        # algorithmic bytes: map 8 B/elem, zip 12, fold 4; int mapIndex 8, fold 4
+        self.parts = {"map": Part("map_f32", n, 1, 2 * b, "f32"), "zip": Part("zip_f32", n, 1, 3 * b, "f32"),
+                      "fold": Part("fold_f32", n, 1, b, "f32"), "mapindex": Part("mapindex_i32", n, 1, 2 * b, "i32"),
+                      "ifold": Part("fold_i32", n, 1, b, "i32")}
+
+    def config(self):
+        return {"workload": f"DA<float> {self.n} map 2.5x+1 / zip a*b+a / fold(+); DA<int> mapIndex x^(i&1023) / fold(+)",
+                "l2": "inputs larger than L2 (1 GiB arrays)"}
+
+    def bytes(self):
+        return sum(p.bytes_per_launch for p in self.parts.values())
+
+    def setup(self):
+        from muesli4_gb300 import workloads as W
+        A = self.A
+        a = W.uniform_f32(self.n, -1, 1, 42)
+        b = W.uniform_f32(self.n, -1, 1, 43)
+        x = W.uniform_i32(self.n, 0, 1000, 44)
+        self.host_in = {}
+        for k, v in (("a", a), ("b", b), ("x", x)):
+            t, h = pinned(v.shape, v.dtype)
+            h[...] = v
+            self.host_in[k] = (t, h)
+        self.host_out = {"z": pinned(a.shape, np.float32), "y": pinned(x.shape, np.int32)}
+        self.dev = {"a": A.DeviceArray.from_host(a), "b": A.DeviceArray.from_host(b), "x": A.DeviceArray.from_host(x),
+                    "m": A.DeviceArray(a.shape, np.float32), "z": A.DeviceArray(a.shape, np.float32),
+                    "y": A.DeviceArray(x.shape, np.int32)}
+        self.h2d = sum(h.nbytes for _, h in self.host_in.values())
+        self.d2h = sum(h.nbytes for _, h in self.host_out.values()) + 8
+
+    def updates(self):
+        return self.bytes()
+
+    def step(self, ev=None, marks=None):
+        A, d = self.A, self.dev
+        A.map(A.MSL_MAP_AFFINE, d["a"], d["m"], (2.5, 1.0))
+        if ev is not None:
+            marks.append(("map", ev.record()))
+        A.zip(A.MSL_ZIP_MULADD, d["m"], d["b"], d["z"])
+        if ev is not None:
+            marks.append(("zip", ev.record()))
+        self.fsum = A.fold(A.MSL_FOLD_SUM, d["z"])
+        if ev is not None:
+            marks.append(("fold", ev.record()))
+        A.map_index(A.MSL_IDX_XOR_MASK, d["x"], d["y"], (1023,))
+        if ev is not None:
+            marks.append(("mapindex", ev.record()))
+        self.isum = A.fold(A.MSL_FOLD_SUM, d["y"])
+        if ev is not None:
+            marks.append(("ifold", ev.record()))
+
+    def e2e_step(self):
+        A, d = self.A, self.dev
+        for k in ("a", "b", "x"):
+            _, h = self.host_in[k]
+            A.check(A.load().msl_upload(d[k].ptr, h.ctypes.data, h.nbytes), "msl_upload")
+        self.step()
+        for k in ("z", "y"):
+            _, h = self.host_out[k]
+            A.check(A.load().msl_download(h.ctypes.data, d[k].ptr, h.nbytes), "msl_download")
+
+    def cpu_sample(self, O, threads, min_seconds: float = 0.0):
+        from muesli4_gb300 import workloads as W
+        n = 1 << 25
+        a = W.uniform_f32(n, -1, 1, 42)
+        b = W.uniform_f32(n, -1, 1, 43)
+        x = W.uniform_i32(n, 0, 1000, 44)
+        O.set_threads(threads)
+        t = {}
+        t0 = time.perf_counter(); m = O.map(0, a, (2.5, 1.0)); t["map"] = time.perf_counter() - t0
+        t0 = time.perf_counter(); z = O.zip(3, m, b); t["zip"] = time.perf_counter() - t0
+        t0 = time.perf_counter(); y = O.map_index(2, x, (1023,)); t["mapindex"] = time.perf_counter() - t0
+        O.set_threads(1)  # the reference's parallel fold is a data race; its correct form is sequential
+        t0 = time.perf_counter(); O.fold(0, z); t["fold"] = time.perf_counter() - t0
+        t0 = time.perf_counter(); O.fold(0, y); t["ifold"] = time.perf_counter() - t0
+        O.set_threads(threads)
+        scale = self.n / n
+        total_t = sum(v * scale for v in t.values())
+        return self.bytes() / total_t / 1e9, f"2^25-element arrays ({threads} threads; folds on 1 thread)"
+
+
+WORKLOADS = {
+    "stencil_suite": lambda A: StencilSuite(A),
+    "box": lambda A: StencilSuite(A, parts=("box",)),
+    "life": lambda A: StencilSuite(A, parts=("life",)),
+    "heat": lambda A: StencilSuite(A, parts=("heat",)),
+    "jacobi": lambda A: Jacobi(A),
+    "mapzipfold": lambda A: MapZipFold(A),
+}
+
+
+def value_of(w, seconds: float) -> float:
+    return w.updates() / seconds / 1e9
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, dist: Dist):
+    """Reference arm: the CPU implementation of the path (the oracle, a
+    restatement of the reference's OpenMP loops) on this host's cores."""
+    if dist.rank != 0:
+        return
+    from oracle import pyoracle as O
+    O.build()
+    w = WORKLOADS[args.workload](None)
+    threads = cpu_threads()
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, sample = w.cpu_sample(O, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    v = statistics.median(vals)
+    line = {"metric": w.metric, "value": v, "unit": w.unit, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": w.dtype, "data": "synthetic", "impl": "reference",
+            "config": w.config() if hasattr(w, "config") else {"workload": args.workload},
+            "cpu_baseline": {"value": v, "unit": w.unit, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": w.unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="stencil_suite", choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+        dist.close()
+        return
+
+    from muesli4_gb300 import abi as A
+    A.init(dist.local_rank)
+    w = WORKLOADS[args.workload](A)
+    w.setup()
+    ev = Events(A)
+    for _ in range(args.warmup):
+        w.step()
+    A.sync()
+
+    # ---- device-resident timed region ----
+    dist.barrier()
+    A.sync()
+    sampler = ClockSampler(dist.local_rank)
+    sampler.start()
+    launches0 = A.launch_count()
+    step_marks = []
+    e0 = ev.record()
+    for _ in range(args.steps):
+        start, marks = ev.record(), []
+        w.step(ev, marks)
+        step_marks.append((start, marks))
+    e1 = ev.record()
+    A.sync()
+    launches = A.launch_count() - launches0
+    clocks = sampler.stop()
+    dist.barrier()
+    total_ms = ev.ms(e0, e1)
+    # per-part device time: from the event before each part to the event after it
+    per_part = {k: 0.0 for k in w.parts}
+    for start, marks in step_marks:
+        prev = start
+        for k, e in marks:
+            per_part[k] += ev.ms(prev, e)
+            prev = e
+    t_max = dist.max(total_ms / 1e3)
+    total_updates = dist.sum(w.updates() * args.steps)
+    value = total_updates / t_max / 1e9
+
+    # ---- end to end through the C ABI with host buffers ----
+    for _ in range(1):
+        w.e2e_step()
+    A.sync()
+    dist.barrier()
+    t0 = time.perf_counter()
+    e_a = ev.record()
+    for _ in range(args.steps):
+        w.e2e_step()
+    e_b = ev.record()
+    A.sync()
+    e2e_s = max(time.perf_counter() - t0, ev.ms(e_a, e_b) / 1e3)
+    e2e_s = dist.max(e2e_s)
+    e2e_value = dist.sum(w.updates() * args.steps) / e2e_s / 1e9
+
+    # ---- roofline of the dominant kernel ----
+    peak, peak_kind = measured_peaks()
+    dom = max(w.parts, key=lambda k: per_part[k])
+    p = w.parts[dom]
+    avg_launch_s = per_part[dom] / 1e3 / (args.steps * p.launches)
+    achieved = p.bytes_per_launch / avg_launch_s / 1e9
+    parts_out = {}
+    for k, pp in w.parts.items():
+        t = per_part[k] / 1e3 / args.steps
+        parts_out[pp.name] = {"ms_per_step": t * 1e3, "launches_per_step": pp.launches,
+                              "GB_per_s": pp.bytes_per_launch * pp.launches / t / 1e9 if t > 0 else None}
+        if w.unit == "GCUPS":
+            parts_out[pp.name]["GCUPS"] = pp.updates / t / 1e9 if t > 0 else None
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get(f"{w.name}:{p.name}")
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        try:
+            from oracle import pyoracle as O
+            O.build()
+            threads = cpu_threads()
+            v, sample = w.cpu_sample(O, threads, min_seconds=10.0)
+            cpu = {"value": v, "unit": w.unit, "cores": threads, "kind": "port", "sample": sample}
+        except Exception as exc:  # the CPU baseline is reported, never required
+            cpu = {"value": None, "unit": w.unit, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
+
+    if dist.rank == 0:
+        line = {
+            "metric": w.metric, "value": value, "unit": w.unit, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": w.dtype, "data": "synthetic",
+            "config": dict(w.config(), parallelism=f"replicas x{dist.world}"),
+            "e2e": {"value": e2e_value, "unit": w.unit, "h2d_bytes_per_step": w.h2d, "d2h_bytes_per_step": w.d2h},
+            "roofline": {"bound": "hbm", "kernel": p.name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                         "bytes_per_launch": p.bytes_per_launch},
+            "parts": parts_out,
+            "cpu_baseline": cpu,
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()
