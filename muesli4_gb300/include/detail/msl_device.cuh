@@ -80,10 +80,10 @@ MSL_HD bf16s f_to_bf16(float f) {  // round to nearest even, NaN stays quiet
 // Storage type S -> arithmetic type used by the stencil functors.
 template <typename S> struct Compute { using type = S; };
 template <> struct Compute<bf16s> { using type = float; };
-template <typename S> MSL_DEV typename Compute<S>::type widen(S s) { return s; }
-template <> MSL_DEV float widen<bf16s>(bf16s s) { return bf16_to_f(s); }
-template <typename S> MSL_DEV S narrow(typename Compute<S>::type v) { return v; }
-template <> MSL_DEV bf16s narrow<bf16s>(float v) { return f_to_bf16(v); }
+template <typename S> MSL_HD typename Compute<S>::type widen(S s) { return s; }
+template <> MSL_HD float widen<bf16s>(bf16s s) { return bf16_to_f(s); }
+template <typename S> MSL_HD S narrow(typename Compute<S>::type v) { return v; }
+template <> MSL_HD bf16s narrow<bf16s>(float v) { return f_to_bf16(v); }
 
 // ---- vectors ---------------------------------------------------------------------
 template <int BYTES> struct RawWord;

@@ -53,7 +53,7 @@ template <typename T, typename S = T> class NPLMatrix {
     int ox_ = 0, oy_ = 0, pitch_ = 0, tile_h_ = 0;
     bool check_ = true;
 
-    __device__ __forceinline__ T operator()(int x, int y) const {
+    __host__ __device__ __forceinline__ T operator()(int x, int y) const {
         const unsigned tx = (unsigned)(x - ox_), ty = (unsigned)(y - oy_);
         if (tx < (unsigned)pitch_ && ty < (unsigned)tile_h_) {
             if (!check_ || ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height))
@@ -77,7 +77,7 @@ template <typename T, typename S = T> class PLCube {
     int ox_ = 0, oy_ = 0, pitch_ = 0, tile_h_ = 0, plane_ = 0, mask_ = 0, zlo_ = 0, zhi_ = -1;
     bool check_ = true;
 
-    __device__ __forceinline__ T operator()(int x, int y, int z) const {
+    __host__ __device__ __forceinline__ T operator()(int x, int y, int z) const {
         const unsigned tx = (unsigned)(x - ox_), ty = (unsigned)(y - oy_);
         if (tx < (unsigned)pitch_ && ty < (unsigned)tile_h_ && z >= zlo_ && z <= zhi_) {
             if (!check_ || ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height &&

@@ -10,10 +10,10 @@ namespace msl {
 
 template <typename T> class PLMatrix {
    public:
-    __device__ __forceinline__ explicit PLMatrix(const NPLMatrix<T> &view) : view_(view) {}
-    __device__ __forceinline__ T get(int row, int col) const { return view_(col, row); }
-    __device__ __forceinline__ int getRows() const { return view_.height; }
-    __device__ __forceinline__ int getCols() const { return view_.width; }
+    __host__ __device__ __forceinline__ explicit PLMatrix(const NPLMatrix<T> &view) : view_(view) {}
+    __host__ __device__ __forceinline__ T get(int row, int col) const { return view_(col, row); }
+    __host__ __device__ __forceinline__ int getRows() const { return view_.height; }
+    __host__ __device__ __forceinline__ int getCols() const { return view_.width; }
 
    private:
     const NPLMatrix<T> &view_;
