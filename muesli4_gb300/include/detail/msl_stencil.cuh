@@ -12,17 +12,21 @@
 //    vertical strip of 8 cells of one column (a warp covers 32 consecutive
 //    columns, so shared-memory reads are conflict-free and global stores are
 //    coalesced).
-//  * 3-D: each CTA owns a 64 x 16 column of the cube for a chunk of planes and
+//  * 3-D: each CTA owns a 64 x 32 column of the cube for a chunk of planes and
 //    marches along z with a ring of shared-memory planes (2r+1 in use, one in
 //    flight), one TMA 3-D load per plane.
 // The functor sees the same view type the reference passes (NPLMatrix /
 // PLCube): public width/height[/depth], neutralValue, stencilSize and
-// operator()(x, y[, z]) that returns neutralValue outside the grid. Reads that
-// hit the staged window come from shared memory; any other read (a functor
-// reaching beyond the radius it declared) falls through to global memory, so
-// the semantics are the reference's for every functor. Tiles whose staged
-// window lies inside the grid run the functor with the bounds test compiled
-// out. Where TMA cannot address the grid (row pitch not a multiple of 16
+// operator()(x, y[, z]) that returns neutralValue outside the grid and reads
+// every other cell from shared memory. As in the reference -- whose halo
+// buffers hold exactly stencilSize rows/planes (include/dm.h:224-291) -- a
+// functor must read only within the radius it declares; defining
+// MSL_STENCIL_CHECK_RADIUS makes the view test that and serve reads beyond the
+// staged window from global memory instead. Tiles whose staged window lies
+// inside the grid run the functor with the bounds test compiled out, so an
+// interior read is one shared-memory load at an offset the compiler can fold
+// and reuse across the vertically adjacent cells a thread computes. Where TMA
+// cannot address the grid (row pitch not a multiple of 16
 // bytes, misaligned base, oversized halo) the same kernel stages the window
 // with plain coalesced loads.
 //
@@ -54,15 +58,16 @@ template <typename T, typename S = T> class NPLMatrix {
     bool check_ = true;
 
     __host__ __device__ __forceinline__ T operator()(int x, int y) const {
+#ifdef MSL_STENCIL_CHECK_RADIUS
         const unsigned tx = (unsigned)(x - ox_), ty = (unsigned)(y - oy_);
-        if (tx < (unsigned)pitch_ && ty < (unsigned)tile_h_) {
-            if (!check_ || ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height))
-                return gpu::widen<S>(tile_[ty * pitch_ + tx]);
+        if (!(tx < (unsigned)pitch_ && ty < (unsigned)tile_h_)) {  // beyond the declared radius
+            if ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height)
+                return gpu::widen<S>(global_[(size_t)y * width + x]);
             return neutralValue;
         }
-        if ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height)
-            return gpu::widen<S>(global_[(size_t)y * width + x]);
-        return neutralValue;
+#endif
+        if (check_ && ((unsigned)x >= (unsigned)width || (unsigned)y >= (unsigned)height)) return neutralValue;
+        return gpu::widen<S>(tile_[(y - oy_) * pitch_ + (x - ox_)]);
     }
 };
 
@@ -78,23 +83,24 @@ template <typename T, typename S = T> class PLCube {
     bool check_ = true;
 
     __host__ __device__ __forceinline__ T operator()(int x, int y, int z) const {
+#ifdef MSL_STENCIL_CHECK_RADIUS
         const unsigned tx = (unsigned)(x - ox_), ty = (unsigned)(y - oy_);
-        if (tx < (unsigned)pitch_ && ty < (unsigned)tile_h_ && z >= zlo_ && z <= zhi_) {
-            if (!check_ || ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height &&
-                            (unsigned)z < (unsigned)depth))
-                return gpu::widen<S>(ring_[(z & mask_) * plane_ + ty * pitch_ + tx]);
+        if (!(tx < (unsigned)pitch_ && ty < (unsigned)tile_h_ && z >= zlo_ && z <= zhi_)) {
+            if ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height && (unsigned)z < (unsigned)depth)
+                return gpu::widen<S>(global_[((size_t)z * height + y) * width + x]);
             return neutralValue;
         }
-        if ((unsigned)x < (unsigned)width && (unsigned)y < (unsigned)height && (unsigned)z < (unsigned)depth)
-            return gpu::widen<S>(global_[((size_t)z * height + y) * width + x]);
-        return neutralValue;
+#endif
+        if (check_ && ((unsigned)x >= (unsigned)width || (unsigned)y >= (unsigned)height || (unsigned)z >= (unsigned)depth))
+            return neutralValue;
+        return gpu::widen<S>(ring_[(z & mask_) * plane_ + (y - oy_) * pitch_ + (x - ox_)]);
     }
 };
 
 namespace gpu {
 
 constexpr int kSt2BX = 64, kSt2BY = 32, kSt2RPT = 8, kSt2Threads = 256;
-constexpr int kSt3BX = 64, kSt3BY = 16, kSt3RPT = 4, kSt3Threads = 256;
+constexpr int kSt3BX = 64, kSt3BY = 32, kSt3RPT = 8, kSt3Threads = 256;
 constexpr int kStHeader = 128;  // mbarriers live in the first 128 bytes of dynamic smem
 
 // Halo in x, rounded up to 16 bytes so that a TMA box starting at x0 - hx keeps
@@ -238,7 +244,24 @@ __global__ void __launch_bounds__(kSt2Threads)
     }
 }
 
-// One CTA = one 64 x 16 column over planes [z_begin, z_end) of its chunk.
+template <typename S, class Fn, class View>
+MSL_DEV void stencil3d_strip(const Fn &fn, const View &c, int x, int ys, int z, int rows, int cols, S *out, bool want,
+                             double &dmax) {
+#pragma unroll
+    for (int j = 0; j < kSt3RPT; j++) {
+        const int y = ys + j;
+        if (y < rows) {
+            const S sv = narrow<S>(fn(c, x, y, z));
+            out[((size_t)z * rows + y) * cols + x] = sv;
+            if (want) {
+                const double d = fabs(stored_f64(sv) - (double)c(x, y, z));
+                if (d > dmax || d != d) dmax = d;
+            }
+        }
+    }
+}
+
+// One CTA = one 64 x 32 column over planes [z_begin, z_end) of its chunk.
 // Ring of NS = 2^k >= 2r+2 plane slots, one mbarrier per slot.
 template <typename S, class Fn, bool TMA>
 __global__ void __launch_bounds__(kSt3Threads)
@@ -330,25 +353,12 @@ __global__ void __launch_bounds__(kSt3Threads)
         c.zhi_ = z + r;
         const bool inside = xy_inside && z - r >= 0 && z + r < depth;
         if (x < cols) {
-            c.check_ = true;
-#pragma unroll
-            for (int j = 0; j < kSt3RPT; j++) {
-                const int y = ys + j;
-                if (y < rows) {
-                    S sv;
-                    if (inside) {
-                        PLCube<T, S> ci = c;
-                        ci.check_ = false;
-                        sv = narrow<S>(fn(ci, x, y, z));
-                    } else {
-                        sv = narrow<S>(fn(c, x, y, z));
-                    }
-                    out[((size_t)z * rows + y) * cols + x] = sv;
-                    if (want) {
-                        const double d = fabs(stored_f64(sv) - (double)c(x, y, z));
-                        if (d > dmax || d != d) dmax = d;
-                    }
-                }
+            if (inside) {
+                c.check_ = false;
+                stencil3d_strip<S>(fn, c, x, ys, z, rows, cols, out, want, dmax);
+            } else {
+                c.check_ = true;
+                stencil3d_strip<S>(fn, c, x, ys, z, rows, cols, out, want, dmax);
             }
         }
     }

@@ -216,10 +216,11 @@ int fe_da_kat(int dim) {
     a.zipInPlace(c, product);
     expect_all("zipInPlace(lambda)", a, 20);
     // host-side element access and copies
-    a.set(1, 99);
-    if (a.get(1) != 99) failures++;
+    const int k = dim - 1;
+    a.set(k, 99);
+    if (a.get(k) != 99) failures++;
     DA<int> copy(a);
-    if (copy.get(1) != 99 || copy.get(0) != 20) failures++;
+    if (copy.get(k) != 99 || (k > 0 && copy.get(0) != 20)) failures++;
     return failures;
 }
 
