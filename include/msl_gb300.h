@@ -165,6 +165,12 @@ int msl_fold_absdiff_max(int dtype, const void *a, const void *b, size_t n, doub
  * identical either way; the switch exists to test and compare the loaders.
  * No reference counterpart (the reference has no staging). */
 int msl_set_tma(int enabled);
+/* Sweeps fused into one launch by msl_stencil2d_iterate (temporal blocking:
+ * the CTA runs depth-1 sweeps on a shared-memory tile with a depth*r halo and
+ * writes the last; results are identical to single sweeps). 0 (default) uses
+ * the autotuner's choice for the grid, or 1 when none was recorded. Applies to
+ * Jacobi, heat2D (F32, F64, BF16) and Life. No reference counterpart. */
+int msl_set_temporal_depth(int depth);
 /* out = f(view, x, y) for every cell of a rows x cols grid; `radius` is the
  * stencil size r, `neutral` the value outside the grid. in != out.
  * DM::mapStencil<f> (src/dm.cpp:1535-1591), NPLMatrix (include/nplmatrix.h:56-168). */
@@ -181,6 +187,19 @@ int msl_stencil3d(int dtype, int kind, const void *in, void *out, int depth, int
                   int radius, double neutral);
 int msl_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int rows, int cols,
                           int radius, double neutral, int iters, double *residual, int *result_in_b);
+
+/* ---- autotuner -------------------------------------------------------------
+ * Times msl_stencil2d_iterate over `iters` sweeps of a rows x cols grid for
+ * every temporal depth that fits (1, 2, 3, 4, 6, 8), on scratch grids it
+ * allocates and frees, records the fastest for (dtype, kind, radius, grid-size
+ * class) and returns it with its rate in cell updates per second. The record
+ * is used by later iterate calls when the temporal depth is 0. No reference
+ * counterpart (the reference fixes tile width 16, include/muesli.h:195). */
+int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, int iters, int *best_depth,
+                           double *best_rate);
+/* Persist / restore the autotuner's records (plain text, one record per line). */
+int msl_autotune_save(const char *path);
+int msl_autotune_load(const char *path);
 
 #ifdef __cplusplus
 }

@@ -68,6 +68,8 @@ def load() -> ctypes.CDLL:
         "msl_stencil2d": [i, i, vp, vp, i, i, i, d], "msl_stencil2d_iterate": [i, i, vp, vp, i, i, i, d, i, dp, ip],
         "msl_stencil3d": [i, i, vp, vp, i, i, i, i, d],
         "msl_stencil3d_iterate": [i, i, vp, vp, i, i, i, i, d, i, dp, ip],
+        "msl_set_temporal_depth": [i], "msl_autotune_stencil2d": [i, i, i, i, i, i, ip, dp],
+        "msl_autotune_save": [ctypes.c_char_p], "msl_autotune_load": [ctypes.c_char_p],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -111,6 +113,27 @@ def launch_count() -> int:
 
 def set_tma(enabled: bool) -> None:
     check(load().msl_set_tma(1 if enabled else 0))
+
+
+def set_temporal_depth(depth: int) -> None:
+    """Sweeps fused per launch by stencil2d_iterate (0 = autotuner's choice)."""
+    check(load().msl_set_temporal_depth(int(depth)), "msl_set_temporal_depth")
+
+
+def autotune_stencil2d(kind: int, dtype: int, rows: int, cols: int, radius: int, iters: int):
+    """Returns (best temporal depth, cell updates per second)."""
+    d, r = ctypes.c_int(), ctypes.c_double()
+    check(load().msl_autotune_stencil2d(dtype, kind, rows, cols, radius, iters, ctypes.byref(d), ctypes.byref(r)),
+          "msl_autotune_stencil2d")
+    return d.value, r.value
+
+
+def autotune_save(path: str) -> None:
+    check(load().msl_autotune_save(path.encode()), "msl_autotune_save")
+
+
+def autotune_load(path: str) -> None:
+    check(load().msl_autotune_load(path.encode()), "msl_autotune_load")
 
 
 def device_info():

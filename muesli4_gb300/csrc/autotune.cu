@@ -1,0 +1,141 @@
+// Autotuner for the stencil skeletons: times the candidate temporal depths of
+// msl_stencil2d_iterate on the caller's grid shape and records the fastest per
+// (element type, functor, radius, grid-size class). The reference fixes its
+// tiling statically (tile width 16, include/muesli.h:195; 1024-thread blocks,
+// src/muesli.cpp:103).
+#include <cmath>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "msl_internal.h"
+
+namespace msl {
+namespace rt {
+
+namespace {
+using Key = std::tuple<int, int, int, int>;  // dtype, kind, radius, size class
+struct Record {
+    int depth;
+    double rate;
+};
+std::mutex g_mu;
+std::map<Key, Record> &table() {
+    static std::map<Key, Record> t;
+    return t;
+}
+// Grid-size class: rounded log2 of the cell count (grids within a factor of
+// sqrt(2) share a record).
+int size_class(int rows, int cols) { return (int)std::lround(std::log2((double)rows * (double)cols)); }
+}  // namespace
+
+int tuned_depth(int dtype, int kind, int rows, int cols, int radius) {
+    std::lock_guard<std::mutex> g(g_mu);
+    auto it = table().find(Key{dtype, kind, radius, size_class(rows, cols)});
+    return it == table().end() ? 1 : it->second.depth;
+}
+
+}  // namespace rt
+}  // namespace msl
+
+using namespace msl;
+
+extern "C" {
+
+int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, int iters, int *best_depth,
+                           double *best_rate) {
+    auto &c = rt::ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    if (int e = rt::require_init()) return e;
+    if (rows <= 0 || cols <= 0 || iters < 1)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_autotune_stencil2d: bad shape or iteration count");
+    const size_t es = rt::dtype_size(dtype);
+    if (!es) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_autotune_stencil2d: unknown dtype %d", dtype);
+    const size_t bytes = (size_t)rows * cols * es;
+    void *a = nullptr, *b = nullptr;
+    MSL_TRY_CUDA(cudaMalloc(&a, bytes), "msl_autotune_stencil2d");
+    if (cudaMalloc(&b, bytes) != cudaSuccess) {
+        cudaFree(a);
+        return rt::fail(MSL_ERR_OUT_OF_MEMORY, "msl_autotune_stencil2d: scratch grids");
+    }
+    // A 0/1 pattern is a valid input for every built-in functor and element type.
+    cudaMemsetAsync(a, 0, bytes, c.stream);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int best = 1;
+    double best_r = 0.0;
+    int rc = MSL_OK;
+    const int saved = 0;
+    const int candidates[] = {1, 2, 3, 4, 6, 8};
+    for (int d : candidates) {
+        if (d > iters) break;
+        if (msl_set_temporal_depth(d) != MSL_OK) continue;
+        int inb = 0;
+        // warm-up, then timed
+        rc = msl_stencil2d_iterate(dtype, kind, a, b, rows, cols, radius, 0.0, d, nullptr, &inb);
+        if (rc != MSL_OK) {
+            if (d == 1) break;  // the functor itself is not available: report it
+            rc = MSL_OK;        // this depth does not fit: skip it
+            continue;
+        }
+        cudaEventRecord(e0, c.stream);
+        rc = msl_stencil2d_iterate(dtype, kind, a, b, rows, cols, radius, 0.0, iters, nullptr, &inb);
+        cudaEventRecord(e1, c.stream);
+        if (rc != MSL_OK) break;
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double rate = (double)rows * cols * iters / (ms * 1e-3);
+        if (rate > best_r) {
+            best_r = rate;
+            best = d;
+        }
+    }
+    msl_set_temporal_depth(saved);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(a);
+    cudaFree(b);
+    if (rc != MSL_OK) return rc;
+    {
+        std::lock_guard<std::mutex> g2(rt::g_mu);
+        rt::table()[rt::Key{dtype, kind, radius, rt::size_class(rows, cols)}] = rt::Record{best, best_r};
+    }
+    if (best_depth) *best_depth = best;
+    if (best_rate) *best_rate = best_r;
+    return rt::check_device_errors("msl_autotune_stencil2d");
+}
+
+int msl_autotune_save(const char *path) {
+    if (!path) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_autotune_save: NULL path");
+    FILE *f = std::fopen(path, "w");
+    if (!f) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_autotune_save: cannot open %s", path);
+    std::lock_guard<std::mutex> g(rt::g_mu);
+    std::fprintf(f, "# dtype kind radius size_class depth rate\n");
+    for (auto &kv : rt::table())
+        std::fprintf(f, "%d %d %d %d %d %.6g\n", std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
+                     std::get<3>(kv.first), kv.second.depth, kv.second.rate);
+    std::fclose(f);
+    return MSL_OK;
+}
+
+int msl_autotune_load(const char *path) {
+    if (!path) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_autotune_load: NULL path");
+    FILE *f = std::fopen(path, "r");
+    if (!f) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_autotune_load: cannot open %s", path);
+    char line[256];
+    std::lock_guard<std::mutex> g(rt::g_mu);
+    while (std::fgets(line, sizeof line, f)) {
+        if (line[0] == '#') continue;
+        int dt, k, r, sc, d;
+        double rate;
+        if (std::sscanf(line, "%d %d %d %d %d %lf", &dt, &k, &r, &sc, &d, &rate) == 6 && d >= 1 && d <= 16)
+            rt::table()[rt::Key{dt, k, r, sc}] = rt::Record{d, rate};
+    }
+    std::fclose(f);
+    return MSL_OK;
+}
+
+}  // extern "C"

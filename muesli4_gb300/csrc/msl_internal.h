@@ -45,6 +45,10 @@ inline void count_launch(unsigned n = 1) { ctx().launches.fetch_add(n, std::memo
 
 size_t dtype_size(int dtype);
 
+// Autotuner table (autotune.cu): sweeps per launch recorded for a 2-D stencil
+// of this element type, functor, radius and grid size; 1 when none is recorded.
+int tuned_depth(int dtype, int kind, int rows, int cols, int radius);
+
 }  // namespace rt
 }  // namespace msl
 

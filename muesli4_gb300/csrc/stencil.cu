@@ -137,20 +137,25 @@ int read_residual(double *residual, const char *what) {
 std::atomic<int> g_tma_enabled{1};
 bool tma_enabled() { return g_tma_enabled.load(std::memory_order_relaxed) != 0; }
 
+// `iters` ping-pong sweeps a -> b -> a ..., `depth` sweeps per launch (the
+// last launch takes the remainder). The residual is fused into the last sweep.
 template <class Launch>
-int iterate(const char *what, void *a, void *b, int iters, double *residual, int *result_in_b, Launch launch) {
+int iterate(const char *what, void *a, void *b, int iters, int depth, double *residual, int *result_in_b,
+            Launch launch) {
     auto &c = ctx();
     Sweep sw{nullptr, tma_enabled()};
     if (residual) MSL_TRY_CUDA(cudaMemsetAsync(c.resid, 0, sizeof(unsigned long long), c.stream), what);
     void *p = a, *q = b;
-    for (int i = 0; i < iters; i++) {
-        sw.resid = (residual && i == iters - 1) ? c.resid : nullptr;
-        cudaError_t e = launch(p, q, sw);
+    for (int i = 0; i < iters;) {
+        const int k = std::min(std::max(depth, 1), iters - i);
+        sw.resid = (residual && i + k == iters) ? c.resid : nullptr;
+        cudaError_t e = launch(p, q, k, sw);
         if (e != cudaSuccess) return rt::cuda_fail(e, what);
         rt::count_launch();
         void *t = p;
         p = q;
         q = t;
+        i += k;
     }
     if (result_in_b) *result_in_b = (p == b);
     if (residual) {
@@ -160,12 +165,29 @@ int iterate(const char *what, void *a, void *b, int iters, double *residual, int
     return MSL_OK;
 }
 
+std::atomic<int> g_temporal_depth{0};
+
+// Sweeps per launch for a 2-D iteration: the fixed setting, or (0) the
+// autotuner's choice recorded for this grid, else 1.
+int depth_for(int dtype, int kind, int rows, int cols, int r) {
+    if (!tb_supported_2d(dtype, kind)) return 1;
+    int d = g_temporal_depth.load(std::memory_order_relaxed);
+    if (d > 0) return d;
+    return msl::rt::tuned_depth(dtype, kind, rows, cols, r);
+}
+
 }  // namespace
 
 extern "C" {
 
 int msl_set_tma(int enabled) {
     g_tma_enabled.store(enabled ? 1 : 0);
+    return MSL_OK;
+}
+
+int msl_set_temporal_depth(int depth) {
+    if (depth < 0 || depth > 16) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_set_temporal_depth: %d not in 0..16", depth);
+    g_temporal_depth.store(depth);
     return MSL_OK;
 }
 
@@ -185,9 +207,15 @@ int msl_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, int c
     if (int e = rt::require_init()) return e;
     if (int e = check2d("msl_stencil2d_iterate", dtype, kind, a, b, rows, cols, radius)) return e;
     if (iters < 1) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_stencil2d_iterate: iters must be >= 1");
-    return iterate("msl_stencil2d_iterate", a, b, iters, residual, result_in_b, [&](void *p, void *q, const Sweep &sw) {
-        return dispatch2d(dtype, kind, p, q, rows, cols, radius, neutral, sw);
-    });
+    const int depth = depth_for(dtype, kind, rows, cols, radius);
+    if (depth > 1 && stencil2d_tb_smem<double>(radius, depth) > kMaxStencilSmem)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_stencil2d_iterate: temporal depth %d too deep for radius %d",
+                        depth, radius);
+    return iterate("msl_stencil2d_iterate", a, b, iters, depth, residual, result_in_b,
+                   [&](void *p, void *q, int k, const Sweep &sw) {
+                       if (k > 1) return tb_sweeps_2d(dtype, kind, p, q, rows, cols, radius, k, neutral, sw.resid, sw.tma);
+                       return dispatch2d(dtype, kind, p, q, rows, cols, radius, neutral, sw);
+                   });
 }
 
 int msl_stencil3d(int dtype, int kind, const void *in, void *out, int depth, int rows, int cols, int radius,
@@ -207,9 +235,10 @@ int msl_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int 
     if (int e = rt::require_init()) return e;
     if (int e = check3d("msl_stencil3d_iterate", dtype, kind, a, b, depth, rows, cols, radius)) return e;
     if (iters < 1) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_stencil3d_iterate: iters must be >= 1");
-    return iterate("msl_stencil3d_iterate", a, b, iters, residual, result_in_b, [&](void *p, void *q, const Sweep &sw) {
-        return dispatch3d(dtype, kind, p, q, depth, rows, cols, radius, neutral, sw);
-    });
+    return iterate("msl_stencil3d_iterate", a, b, iters, 1, residual, result_in_b,
+                   [&](void *p, void *q, int, const Sweep &sw) {
+                       return dispatch3d(dtype, kind, p, q, depth, rows, cols, radius, neutral, sw);
+                   });
 }
 
 }  // extern "C"

@@ -24,7 +24,9 @@ template <typename T, class V> __device__ __forceinline__ T heat5(const V &m, in
     v = Arith<T>::add(v, m(x + 1, y));
     v = Arith<T>::add(v, m(x, y - 1));
     v = Arith<T>::add(v, m(x, y + 1));
-    return div_rn<T>(v, T(4));
+    // v / 4 and v * 0.25 are the same real number, each rounded once: the
+    // results are identical for every v, and the product is one instruction.
+    return Arith<T>::mul(v, T(0.25));
 }
 template <typename T> struct StHeat5 {
     template <class V> __device__ __forceinline__ T operator()(const V &m, int x, int y) const { return heat5<T>(m, x, y); }
@@ -126,5 +128,15 @@ template <int R>
 cudaError_t box_fixed_f32(const float *in, float *out, int rows, int cols, float neutral, bool mean,
                           unsigned long long *resid, bool tma);
 
+}  // namespace builtin
+}  // namespace msl
+
+namespace msl {
+namespace builtin {
+// `depth` fused sweeps (temporal blocking) of a built-in 2-D stencil; defined
+// in stencil_tb.cu for Jacobi / heat2D (F32, F64, BF16) and Life (I32).
+cudaError_t tb_sweeps_2d(int dtype, int kind, const void *in, void *out, int rows, int cols, int r, int depth,
+                         double neutral, unsigned long long *resid, bool tma);
+bool tb_supported_2d(int dtype, int kind);
 }  // namespace builtin
 }  // namespace msl

@@ -142,40 +142,36 @@ MSL_DEV double block_max(double v) {
 template <typename S> MSL_DEV double stored_f64(S s) { return (double)s; }
 template <> MSL_DEV double stored_f64<bf16s>(bf16s s) { return (double)bf16_to_f(s); }
 
-template <typename S, class Fn, class View>
+// The kSt2RPT vertically adjacent outputs of one thread. All values are
+// computed before any is stored: the stores go to global memory, which the
+// compiler cannot prove disjoint from the staged tile, so computing first lets
+// it share the tile loads of neighbouring outputs. FULL: the whole strip lies
+// inside the grid (interior tiles), so no row/column guards are needed.
+template <typename S, bool FULL, class Fn, class View>
 MSL_DEV void stencil2d_strip(const Fn &fn, const View &m, int x, int ys, int rows, int cols, S *out, bool want,
                              double &dmax) {
     using T = typename Compute<S>::type;
-    if (x >= cols) return;
+    if (!FULL && x >= cols) return;
+    T vals[kSt2RPT];
     if constexpr (has_strip2<Fn>::value) {
-        T vals[kSt2RPT];
         fn.strip(m, x, ys, vals);
-#pragma unroll
-        for (int j = 0; j < kSt2RPT; j++) {
-            const int y = ys + j;
-            if (y < rows) {
-                const S sv = narrow<S>(vals[j]);
-                out[(size_t)y * cols + x] = sv;
-                if (want) {
-                    const double d = fabs(stored_f64(sv) - (double)m(x, y));
-                    if (d > dmax || d != d) dmax = d;
-                }
-            }
-        }
     } else {
 #pragma unroll
-        for (int j = 0; j < kSt2RPT; j++) {
-            const int y = ys + j;
-            if (y < rows) {
-                const S sv = narrow<S>(fn(m, x, y));
-                out[(size_t)y * cols + x] = sv;
-                if (want) {
-                    const double d = fabs(stored_f64(sv) - (double)m(x, y));
-                    if (d > dmax || d != d) dmax = d;
-                }
-            }
-        }
+        for (int j = 0; j < kSt2RPT; j++)
+            if (FULL || ys + j < rows) vals[j] = fn(m, x, ys + j);
     }
+    if (want) {
+#pragma unroll
+        for (int j = 0; j < kSt2RPT; j++)
+            if (FULL || ys + j < rows) {
+                const double d = fabs(stored_f64(narrow<S>(vals[j])) - (double)m(x, ys + j));
+                if (d > dmax || d != d) dmax = d;
+            }
+    }
+    S *o = out + (size_t)ys * cols + x;
+#pragma unroll
+    for (int j = 0; j < kSt2RPT; j++)
+        if (FULL || ys + j < rows) o[(size_t)j * cols] = narrow<S>(vals[j]);
 }
 
 // One CTA = one 64 x 32 output block. Dynamic smem: [0,128) mbarrier, then the
@@ -233,10 +229,10 @@ __global__ void __launch_bounds__(kSt2Threads)
     double dmax = 0.0;
     if (interior) {
         m.check_ = false;
-        stencil2d_strip<S>(fn, m, x, ys, rows, cols, out, want, dmax);
+        stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, want, dmax);
     } else {
         m.check_ = true;
-        stencil2d_strip<S>(fn, m, x, ys, rows, cols, out, want, dmax);
+        stencil2d_strip<S, false>(fn, m, x, ys, rows, cols, out, want, dmax);
     }
     if (want) {
         dmax = block_max(dmax);
@@ -244,30 +240,144 @@ __global__ void __launch_bounds__(kSt2Threads)
     }
 }
 
-template <typename S, class Fn, class View>
-MSL_DEV void stencil3d_strip(const Fn &fn, const View &c, int x, int ys, int z, int rows, int cols, S *out, bool want,
-                             double &dmax) {
-#pragma unroll
-    for (int j = 0; j < kSt3RPT; j++) {
-        const int y = ys + j;
-        if (y < rows) {
-            const S sv = narrow<S>(fn(c, x, y, z));
-            out[((size_t)z * rows + y) * cols + x] = sv;
-            if (want) {
-                const double d = fabs(stored_f64(sv) - (double)c(x, y, z));
-                if (d > dmax || d != d) dmax = d;
-            }
+// Temporal blocking: `depth` sweeps of the same functor in one launch. The
+// CTA stages its 64 x 32 output block plus a halo of depth*r cells, runs
+// depth-1 sweeps in shared memory on shrinking regions (ping-pong between two
+// buffers) and writes the last one to global memory. Cells outside the grid
+// are never computed: the view returns the neutral value for them, exactly as
+// it does between separate launches, so the result is bit-identical to
+// `depth` single sweeps while HBM sees one read and one write per `depth`
+// sweeps.
+template <typename S, class Fn, bool TMA>
+__global__ void __launch_bounds__(kSt2Threads)
+    stencil2d_tb_kernel(const __grid_constant__ CUtensorMap tmap, const S *in, S *out, int rows, int cols, int r,
+                        int depth, int hx, typename Compute<S>::type neutral, Fn fn, unsigned long long *resid,
+                        unsigned *err) {
+    using T = typename Compute<S>::type;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
+    const int pitch = kSt2BX + 2 * hx, th = kSt2BY + 2 * depth * r;
+    const int buf_elems = (pitch * th * (int)sizeof(S) + 127) / 128 * 128 / (int)sizeof(S);
+    S *buf0 = reinterpret_cast<S *>(smem_raw + kStHeader);
+    S *buf1 = buf0 + buf_elems;
+    const int x0 = blockIdx.x * kSt2BX, y0 = blockIdx.y * kSt2BY;
+    const int wx0 = x0 - hx, wy0 = y0 - depth * r;
+    bool ok = true;
+    if constexpr (TMA) {
+        if (threadIdx.x == 0) {
+            mbar_init(bar, 1);
+            fence_barrier_init();
         }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_arrive_expect_tx(bar, (uint32_t)(pitch * th * sizeof(S)));
+            tma_load_2d(buf0, &tmap, bar, wx0, wy0);
+        }
+        ok = mbar_wait_bounded(bar, 0, err);
+    } else {
+        for (int i = threadIdx.x; i < pitch * th; i += blockDim.x) {
+            const int ty = i / pitch, tx = i - ty * pitch;
+            const int gx = wx0 + tx, gy = wy0 + ty;
+            buf0[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows) ? in[(size_t)gy * cols + gx] : S{};
+        }
+    }
+    ok = __syncthreads_and(ok);
+    if (!ok) return;
+
+    NPLMatrix<T, S> m;
+    m.width = cols;
+    m.height = rows;
+    m.stencilSize = r;
+    m.neutralValue = neutral;
+    m.tile_ = buf0;
+    m.global_ = in;
+    m.ox_ = wx0;
+    m.oy_ = wy0;
+    m.pitch_ = pitch;
+    m.tile_h_ = th;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    S *dst = buf1;
+    for (int s = 1; s < depth; s++) {
+        const int ext = (depth - s) * r;  // halo the remaining sweeps still need
+        const int W = kSt2BX + 2 * ext, H = kSt2BY + 2 * ext;
+        const int gx0 = x0 - ext, gy0 = y0 - ext;
+        const bool interior = gx0 - r >= 0 && gy0 - r >= 0 && gx0 + W + r <= cols && gy0 + H + r <= rows;
+        auto sweep = [&](const NPLMatrix<T, S> &v) {
+            for (int row = warp; row < H; row += nwarps) {
+                const int gy = gy0 + row;
+                if ((unsigned)gy >= (unsigned)rows) continue;
+                for (int col = lane; col < W; col += 32) {
+                    const int gx = gx0 + col;
+                    if ((unsigned)gx < (unsigned)cols) dst[(gy - wy0) * pitch + (gx - wx0)] = narrow<S>(fn(v, gx, gy));
+                }
+            }
+        };
+        if (interior) {
+            m.check_ = false;
+            sweep(m);
+        } else {
+            m.check_ = true;
+            sweep(m);
+        }
+        __syncthreads();
+        m.tile_ = dst;
+        dst = (dst == buf1) ? buf0 : buf1;
+    }
+    const int x = x0 + (warp % (kSt2BX / 32)) * 32 + lane;
+    const int ys = y0 + (warp / (kSt2BX / 32)) * kSt2RPT;
+    const bool interior = x0 - r >= 0 && y0 - r >= 0 && x0 + kSt2BX + r <= cols && y0 + kSt2BY + r <= rows;
+    const bool want = resid != nullptr;
+    double dmax = 0.0;
+    if (interior) {
+        m.check_ = false;
+        stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, want, dmax);
+    } else {
+        m.check_ = true;
+        stencil2d_strip<S, false>(fn, m, x, ys, rows, cols, out, want, dmax);
+    }
+    if (want) {
+        dmax = block_max(dmax);
+        if (threadIdx.x == 0) atomic_max_nonneg(resid, dmax);
     }
 }
 
-// One CTA = one 64 x 32 column over planes [z_begin, z_end) of its chunk.
-// Ring of NS = 2^k >= 2r+2 plane slots, one mbarrier per slot.
+// kSt3RPT vertically adjacent outputs of plane z; computed before stored (see stencil2d_strip).
+template <typename S, bool FULL, class Fn, class View>
+MSL_DEV void stencil3d_strip(const Fn &fn, const View &c, int x, int ys, int z, int rows, int cols, S *out, bool want,
+                             double &dmax) {
+    using T = typename Compute<S>::type;
+    if (!FULL && x >= cols) return;
+    T vals[kSt3RPT];
+#pragma unroll
+    for (int j = 0; j < kSt3RPT; j++)
+        if (FULL || ys + j < rows) vals[j] = fn(c, x, ys + j, z);
+    if (want) {
+#pragma unroll
+        for (int j = 0; j < kSt3RPT; j++)
+            if (FULL || ys + j < rows) {
+                const double d = fabs(stored_f64(narrow<S>(vals[j])) - (double)c(x, ys + j, z));
+                if (d > dmax || d != d) dmax = d;
+            }
+    }
+    S *o = out + ((size_t)z * rows + ys) * cols + x;
+#pragma unroll
+    for (int j = 0; j < kSt3RPT; j++)
+        if (FULL || ys + j < rows) o[(size_t)j * cols] = narrow<S>(vals[j]);
+}
+
+// Persistent 3-D kernel. The cube is cut into 64 x 32 (x, y) tiles; the
+// tile-planes (tile, z) are numbered tile-major and every CTA takes an equal
+// contiguous range of them, so all CTAs are resident and finish together
+// (no partial last wave). A range is one or more z-segments of tiles; each
+// segment is a z-march with a ring of NS = 2^k >= 2r+2 shared-memory planes,
+// one TMA 3-D load per plane issued one plane ahead, one mbarrier per slot
+// (its phase tracked in a bit mask). Only the first 2r planes of a segment are
+// re-read halo.
 template <typename S, class Fn, bool TMA>
 __global__ void __launch_bounds__(kSt3Threads)
     stencil3d_kernel(const __grid_constant__ CUtensorMap tmap, const S *in, S *out, int depth, int rows, int cols,
-                     int r, int hx, int ns_log2, int zchunk, typename Compute<S>::type neutral, Fn fn,
-                     unsigned long long *resid, unsigned *err) {
+                     int r, int hx, int ns_log2, typename Compute<S>::type neutral, Fn fn, unsigned long long *resid,
+                     unsigned *err) {
     using T = typename Compute<S>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw);  // up to 16 slots
@@ -275,90 +385,101 @@ __global__ void __launch_bounds__(kSt3Threads)
     const int NS = 1 << ns_log2, mask = NS - 1;
     const int pitch = kSt3BX + 2 * hx, th = kSt3BY + 2 * r;
     const int plane = (pitch * th + 31) / 32 * 32;  // keeps every slot 128-byte aligned
-    const int x0 = blockIdx.x * kSt3BX, y0 = blockIdx.y * kSt3BY;
-    const int wx0 = x0 - hx, wy0 = y0 - r;
-    const int zb = blockIdx.z * zchunk;
-    const int ze = min(depth, zb + zchunk);
-    if (zb >= ze) return;
-    const int pfirst = zb - r;  // planes pfirst .. ze-1+r are loaded, in order
     const uint32_t plane_bytes = (uint32_t)(pitch * th * sizeof(S));
+    const int tiles_x = (cols + kSt3BX - 1) / kSt3BX, tiles_y = (rows + kSt3BY - 1) / kSt3BY;
+    const long long total = (long long)tiles_x * tiles_y * depth;
+    const long long begin = total * blockIdx.x / gridDim.x, end = total * (blockIdx.x + 1) / gridDim.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool want = resid != nullptr;
+    double dmax = 0.0;
+    unsigned phase = 0;  // bit s: parity of the next completion of slot s
 
-    auto slot_of = [&](int p) { return p & mask; };
-    auto parity_of = [&](int p) { return (uint32_t)(((p - pfirst) >> ns_log2) & 1); };
-    auto issue = [&](int p) {  // thread 0 only (TMA) / all threads (plain loads)
-        S *dst = ring + slot_of(p) * plane;
-        if constexpr (TMA) {
-            fence_proxy_async_smem();
-            mbar_arrive_expect_tx(&bars[slot_of(p)], plane_bytes);
-            tma_load_3d(dst, &tmap, &bars[slot_of(p)], wx0, wy0, p);
-        } else {
-            for (int i = threadIdx.x; i < pitch * th; i += blockDim.x) {
-                const int ty = i / pitch, tx = i - ty * pitch;
-                const int gx = wx0 + tx, gy = wy0 + ty;
-                dst[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows && p >= 0 && p < depth)
-                             ? in[((size_t)p * rows + gy) * cols + gx]
-                             : S{};
-            }
-        }
-    };
-
-    bool ok = true;
     if constexpr (TMA) {
         if (threadIdx.x == 0) {
             for (int s = 0; s < NS; s++) mbar_init(&bars[s], 1);
             fence_barrier_init();
         }
-        __syncthreads();
-        if (threadIdx.x == 0)
-            for (int p = pfirst; p <= zb + r; p++) issue(p);  // planes zb-r .. zb+r (2r+1 distinct slots)
-        for (int p = pfirst; p < zb + r && ok; p++) ok = mbar_wait_bounded(&bars[slot_of(p)], parity_of(p), err);
-    } else {
-        for (int p = pfirst; p < zb + r; p++) issue(p);
     }
+    bool ok = true;
+    for (long long pos = begin; pos < end && ok;) {
+        const int tile = (int)(pos / depth);
+        const int zb = (int)(pos % depth);
+        const int ze = (int)min((long long)depth, zb + (end - pos));
+        pos += ze - zb;
+        const int x0 = (tile % tiles_x) * kSt3BX, y0 = (tile / tiles_x) * kSt3BY;
+        const int wx0 = x0 - hx, wy0 = y0 - r;
 
-    PLCube<T, S> c;
-    c.width = cols;
-    c.height = rows;
-    c.depth = depth;
-    c.stencilSize = r;
-    c.neutralValue = neutral;
-    c.ring_ = ring;
-    c.global_ = in;
-    c.ox_ = wx0;
-    c.oy_ = wy0;
-    c.pitch_ = pitch;
-    c.tile_h_ = th;
-    c.plane_ = plane;
-    c.mask_ = mask;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int x = x0 + (warp % (kSt3BX / 32)) * 32 + lane;
-    const int ys = y0 + (warp / (kSt3BX / 32)) * kSt3RPT;
-    const bool xy_inside = wx0 >= 0 && wy0 >= 0 && wx0 + pitch <= cols && wy0 + th <= rows;
-    const bool want = resid != nullptr;
-    double dmax = 0.0;
+        auto issue = [&](int p) {  // thread 0 only (TMA) / all threads (plain loads)
+            S *dst = ring + (p & mask) * plane;
+            if constexpr (TMA) {
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&bars[p & mask], plane_bytes);
+                tma_load_3d(dst, &tmap, &bars[p & mask], wx0, wy0, p);
+            } else {
+                for (int i = threadIdx.x; i < pitch * th; i += blockDim.x) {
+                    const int ty = i / pitch, tx = i - ty * pitch;
+                    const int gx = wx0 + tx, gy = wy0 + ty;
+                    dst[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows && p >= 0 && p < depth)
+                                 ? in[((size_t)p * rows + gy) * cols + gx]
+                                 : S{};
+                }
+            }
+        };
+        auto wait = [&](int p) {
+            const int sl = p & mask;
+            const bool done = mbar_wait_bounded(&bars[sl], (phase >> sl) & 1u, err);
+            phase ^= 1u << sl;
+            return done;
+        };
 
-    for (int z = zb; z < ze; z++) {
-        __syncthreads();  // every thread is done with plane z-r-1's slot
-        const int pn = z + r;      // newest plane output z needs
-        const int pf = z + r + 1;  // plane to prefetch (reuses the slot of z-r-1)
+        __syncthreads();  // the previous segment's readers are done with the ring
         if constexpr (TMA) {
-            if (threadIdx.x == 0 && pf <= ze - 1 + r) issue(pf);
-            ok = ok && mbar_wait_bounded(&bars[slot_of(pn)], parity_of(pn), err);
+            if (threadIdx.x == 0)
+                for (int p = zb - r; p <= zb + r; p++) issue(p);  // 2r+1 distinct slots
+            for (int p = zb - r; p < zb + r; p++) ok = wait(p) && ok;
         } else {
-            issue(pn);
-            __syncthreads();
+            for (int p = zb - r; p < zb + r; p++) issue(p);
         }
-        if (!__syncthreads_and(ok)) return;
-        c.zlo_ = z - r;
-        c.zhi_ = z + r;
-        const bool inside = xy_inside && z - r >= 0 && z + r < depth;
-        if (x < cols) {
-            if (inside) {
+
+        PLCube<T, S> c;
+        c.width = cols;
+        c.height = rows;
+        c.depth = depth;
+        c.stencilSize = r;
+        c.neutralValue = neutral;
+        c.ring_ = ring;
+        c.global_ = in;
+        c.ox_ = wx0;
+        c.oy_ = wy0;
+        c.pitch_ = pitch;
+        c.tile_h_ = th;
+        c.plane_ = plane;
+        c.mask_ = mask;
+        const int x = x0 + (warp % (kSt3BX / 32)) * 32 + lane;
+        const int ys = y0 + (warp / (kSt3BX / 32)) * kSt3RPT;
+        const bool xy_inside = wx0 >= 0 && wy0 >= 0 && wx0 + pitch <= cols && wy0 + th <= rows;
+
+        for (int z = zb; z < ze; z++) {
+            __syncthreads();  // every thread is done with plane z-r-1's slot
+            if constexpr (TMA) {
+                if (threadIdx.x == 0 && z + r + 1 <= ze - 1 + r) issue(z + r + 1);
+                ok = wait(z + r) && ok;
+            } else {
+                issue(z + r);
+                __syncthreads();
+            }
+            if (!__syncthreads_and(ok)) {
+                ok = false;
+                break;
+            }
+            c.zlo_ = z - r;
+            c.zhi_ = z + r;
+            if (xy_inside && z - r >= 0 && z + r < depth) {
                 c.check_ = false;
-                stencil3d_strip<S>(fn, c, x, ys, z, rows, cols, out, want, dmax);
+                stencil3d_strip<S, true>(fn, c, x, ys, z, rows, cols, out, want, dmax);
             } else {
                 c.check_ = true;
-                stencil3d_strip<S>(fn, c, x, ys, z, rows, cols, out, want, dmax);
+                stencil3d_strip<S, false>(fn, c, x, ys, z, rows, cols, out, want, dmax);
             }
         }
     }
@@ -447,6 +568,44 @@ cudaError_t launch_stencil2d(const S *in, S *out, int rows, int cols, int r, typ
     return cudaGetLastError();
 }
 
+template <typename S> inline size_t stencil2d_tb_smem(int r, int depth) {
+    const int pitch = kSt2BX + 2 * halo_x<S>(depth * r), th = kSt2BY + 2 * depth * r;
+    const size_t buf = ((size_t)pitch * th * sizeof(S) + 127) / 128 * 128;
+    return (size_t)kStHeader + 2 * buf;
+}
+
+// `depth` fused sweeps in -> out (depth >= 2; depth 1 is launch_stencil2d).
+template <typename S, class Fn>
+cudaError_t launch_stencil2d_tb(const S *in, S *out, int rows, int cols, int r, int depth,
+                                typename Compute<S>::type neutral, Fn fn, unsigned long long *resid, unsigned *err,
+                                cudaStream_t st, bool allow_tma = true) {
+    const int hx = halo_x<S>(depth * r);
+    const int pitch = kSt2BX + 2 * hx, th = kSt2BY + 2 * depth * r;
+    const size_t smem = stencil2d_tb_smem<S>(r, depth);
+    if (smem > kMaxStencilSmem) return cudaErrorInvalidValue;
+    dim3 grid((cols + kSt2BX - 1) / kSt2BX, (rows + kSt2BY - 1) / kSt2BY);
+    CUtensorMap map{};
+    const bool tma = allow_tma && stencil_tma_ok<S>(in, cols, pitch, th);
+    if (tma) {
+        cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+        cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(S)};
+        cuuint32_t box[2] = {(cuuint32_t)pitch, (cuuint32_t)th};
+        cuuint32_t estr[2] = {1, 1};
+        if (tensor_map_encoder()(&map, tmap_dtype<S>(), 2, const_cast<S *>(in), dims, strides, box, estr,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+        auto k = stencil2d_tb_kernel<S, Fn, true>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, kSt2Threads, smem, st>>>(map, in, out, rows, cols, r, depth, hx, neutral, fn, resid, err);
+    } else {
+        auto k = stencil2d_tb_kernel<S, Fn, false>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, kSt2Threads, smem, st>>>(map, in, out, rows, cols, r, depth, hx, neutral, fn, resid, err);
+    }
+    return cudaGetLastError();
+}
+
 template <typename S, class Fn>
 cudaError_t launch_stencil3d(const S *in, S *out, int depth, int rows, int cols, int r,
                              typename Compute<S>::type neutral, Fn fn, unsigned long long *resid, unsigned *err,
@@ -457,20 +616,19 @@ cudaError_t launch_stencil3d(const S *in, S *out, int depth, int rows, int cols,
     if ((1 << ns_log2) > kStHeader / 8) return cudaErrorInvalidValue;  // mbarrier slots
     const size_t smem = stencil3d_smem<S>(r);
     if (smem > kMaxStencilSmem) return cudaErrorInvalidValue;
-    const long long tiles = (long long)((cols + kSt3BX - 1) / kSt3BX) * ((rows + kSt3BY - 1) / kSt3BY);
-    // Enough CTAs for ~6 per SM, with chunks long enough that the 2r extra
-    // planes per chunk stay a small overhead.
-    long long target = (long long)(sm_count > 0 ? sm_count : 152) * 6;
-    long long nchunks = (target + tiles - 1) / tiles;
-    long long min_len = 8LL * (2 * r + 1);
-    long long max_chunks = (depth + min_len - 1) / min_len;
-    if (nchunks > max_chunks) nchunks = max_chunks;
-    if (nchunks < 1) nchunks = 1;
-    const int zchunk = (int)((depth + nchunks - 1) / nchunks);
-    nchunks = (depth + zchunk - 1) / zchunk;
-    dim3 grid((cols + kSt3BX - 1) / kSt3BX, (rows + kSt3BY - 1) / kSt3BY, (unsigned)nchunks);
+    const long long total = (long long)((cols + kSt3BX - 1) / kSt3BX) * ((rows + kSt3BY - 1) / kSt3BY) * depth;
     CUtensorMap map{};
     const bool tma = allow_tma && stencil_tma_ok<S>(in, cols, pitch, th);
+    auto k = tma ? stencil3d_kernel<S, Fn, true> : stencil3d_kernel<S, Fn, false>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // One wave of resident CTAs, each with at least 8 tile-planes of work.
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kSt3Threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    long long grid = (long long)per_sm * (sm_count > 0 ? sm_count : 152);
+    const long long by_work = (total + 7) / 8;
+    if (grid > by_work) grid = by_work;
+    if (grid < 1) grid = 1;
     if (tma) {
         cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)depth};
         cuuint64_t strides[2] = {(cuuint64_t)cols * sizeof(S), (cuuint64_t)cols * rows * sizeof(S)};
@@ -480,16 +638,9 @@ cudaError_t launch_stencil3d(const S *in, S *out, int depth, int rows, int cols,
                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return cudaErrorInvalidValue;
-        auto k = stencil3d_kernel<S, Fn, true>;
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, kSt3Threads, smem, st>>>(map, in, out, depth, rows, cols, r, hx, ns_log2, zchunk, neutral, fn,
-                                            resid, err);
-    } else {
-        auto k = stencil3d_kernel<S, Fn, false>;
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, kSt3Threads, smem, st>>>(map, in, out, depth, rows, cols, r, hx, ns_log2, zchunk, neutral, fn,
-                                            resid, err);
     }
+    k<<<(unsigned)grid, kSt3Threads, smem, st>>>(map, in, out, depth, rows, cols, r, hx, ns_log2, neutral, fn, resid,
+                                                 err);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,95 @@
+"""Temporal blocking (several sweeps per launch) and the autotuner.
+
+Fused sweeps must be bit-identical to single sweeps: the oracle runs one sweep
+at a time. Shapes include grids smaller than the staged window (every tile is
+a boundary tile) and widths TMA cannot address.
+"""
+import numpy as np
+import pytest
+
+from muesli4_gb300 import workloads as W
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def depth(gpu):
+    yield gpu.set_temporal_depth
+    gpu.set_temporal_depth(0)
+    gpu.set_tma(True)
+
+
+def bits_equal(a, b):
+    return a.shape == b.shape and a.dtype == b.dtype and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+@pytest.mark.parametrize("d", [2, 3, 4, 8])
+@pytest.mark.parametrize("shape", [(3, 5), (33, 47), (64, 64), (130, 200), (257, 1000)], ids=str)
+@pytest.mark.parametrize("tma", [True, False], ids=["tma", "plain"])
+def test_jacobi_fused_sweeps(gpu, depth, d, shape, tma):
+    depth(d)
+    gpu.set_tma(tma)
+    g = W.jacobi_grid(*shape, seed=d)
+    a, b = gpu.DeviceArray.from_host(g), gpu.DeviceArray(g.shape, g.dtype)
+    iters = 3 * d + 1  # full fused launches plus a remainder
+    last, res = gpu.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, a, b, 1, 0.0, iters)
+    want, _, want_res = O.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, g, 1, 0.0, iters)
+    assert bits_equal(last.download(), want)
+    assert res == want_res
+
+
+@pytest.mark.parametrize("d", [2, 4, 6])
+def test_heat2d_fused_with_neutral(gpu, depth, d):
+    depth(d)
+    x = np.random.default_rng(d).random((97, 300), dtype=np.float32)
+    a, b = gpu.DeviceArray.from_host(x), gpu.DeviceArray(x.shape, x.dtype)
+    last, res = gpu.stencil2d_iterate(gpu.MSL_ST2_HEAT5, a, b, 1, 0.75, 2 * d)
+    want, _, want_res = O.stencil2d_iterate(gpu.MSL_ST2_HEAT5, x, 1, 0.75, 2 * d)
+    assert bits_equal(last.download(), want)
+    assert res == want_res
+
+
+@pytest.mark.parametrize("d", [2, 4, 8])
+@pytest.mark.parametrize("shape", [(64, 80), (1000, 1024)], ids=str)
+def test_life_fused(gpu, depth, d, shape):
+    depth(d)
+    board = W.life_board(*shape, seed=d)
+    a, b = gpu.DeviceArray.from_host(board), gpu.DeviceArray(board.shape, np.int32)
+    last, _ = gpu.stencil2d_iterate(gpu.MSL_ST2_LIFE, a, b, 1, 0, 4 * d + 3, residual=False)
+    assert bits_equal(last.download(), O.stencil2d_iterate(gpu.MSL_ST2_LIFE, board, 1, 0, 4 * d + 3)[0])
+
+
+def test_bf16_fused(gpu, depth):
+    depth(4)
+    h = O.to_bf16(W.jacobi_grid(96, 128, 42))
+    a, b = gpu.DeviceArray.from_host(h), gpu.DeviceArray(h.shape, np.uint16)
+    last, res = gpu.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, a, b, 1, 0.0, 9)
+    want, _, want_res = O.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, h, 1, 0.0, 9)
+    assert bits_equal(last.download(), want)
+    assert res == want_res
+
+
+def test_too_deep_is_an_error(gpu, depth):
+    """depth 16 at radius 8 needs a 288-row window: rejected, nothing launched."""
+    depth(16)
+    x = gpu.DeviceArray((64, 64), np.float32)
+    y = gpu.DeviceArray((64, 64), np.float32)
+    with pytest.raises(gpu.MslError) as e:
+        gpu.stencil2d_iterate(gpu.MSL_ST2_HEAT5, x, y, 8, 0.0, 20)
+    assert e.value.code == gpu.MSL_ERR_INVALID_ARGUMENT
+
+
+def test_autotuner_records_and_is_used(gpu, depth, tmp_path):
+    best, rate = gpu.autotune_stencil2d(gpu.MSL_ST2_JACOBI5, gpu.MSL_F32, 1024, 1024, 1, 64)
+    assert best in (1, 2, 3, 4, 6, 8) and rate > 0
+    path = str(tmp_path / "tune.txt")
+    gpu.autotune_save(path)
+    gpu.autotune_load(path)
+    depth(0)  # use the record
+    g = W.jacobi_grid(1024, 1024, 42)
+    a, b = gpu.DeviceArray.from_host(g), gpu.DeviceArray(g.shape, g.dtype)
+    last, res = gpu.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, a, b, 1, 0.0, 50)
+    want, _, want_res = O.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, g, 1, 0.0, 50)
+    assert bits_equal(last.download(), want)
+    assert res == want_res
