@@ -159,6 +159,22 @@ int msl_fold(int dtype, int op, const void *in, size_t n, void *result);
  * one pass; examples/jacobisolver.cpp:127-140 runs them as two skeletons). */
 int msl_fold_absdiff_max(int dtype, const void *a, const void *b, size_t n, double *result);
 
+/* Fold that allocates nothing, for callers that cannot allocate device memory
+ * (code enqueuing work during a CUDA-graph stream capture, loops that must
+ * never pay cudaMalloc's implicit synchronisation, hosts whose device memory
+ * belongs to another allocator). It needs no msl_init: it runs on the current
+ * device and `stream` (a cudaStream_t; NULL is the default stream) and writes
+ * one element of dtype to the device pointer result_device; the caller
+ * synchronises. Its scratch is a static device array of 2048 CTA partials
+ * (about 41 KiB, held by every device that loads the library until exit), so n
+ * is limited to 2^30 elements; larger n fails with MSL_ERR_SIZE_MISMATCH
+ * before anything is launched. The first call on each device looks up the
+ * array's device address (make that first call before any stream capture).
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. dtype MSL_F32, MSL_F64 or MSL_I32; op as msl_fold.
+ * No counterpart in the reference (its fold allocates per call, src/ds.cpp:772). */
+int msl_fold_noalloc(int dtype, int op, const void *in, size_t n, void *result_device, void *stream);
+
 /* ---- stencils ------------------------------------------------------------- */
 /* Stage stencil windows with TMA tensor copies when the grid allows it (1,
  * the default) or always with plain coalesced loads (0). Results are

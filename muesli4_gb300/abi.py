@@ -70,6 +70,7 @@ def load() -> ctypes.CDLL:
         "msl_stencil3d_iterate": [i, i, vp, vp, i, i, i, i, d, i, dp, ip],
         "msl_set_temporal_depth": [i], "msl_autotune_stencil2d": [i, i, i, i, i, i, ip, dp],
         "msl_autotune_save": [ctypes.c_char_p], "msl_autotune_load": [ctypes.c_char_p],
+        "msl_fold_noalloc": [i, i, vp, sz, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
