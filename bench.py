@@ -246,6 +246,15 @@ class StencilSuite:
             self.dev["heat"] = [A.DeviceArray.from_host(cube), A.DeviceArray(cube.shape, np.float32)]
         self.h2d = sum(h.nbytes for _, h in self.host_in.values())
         self.d2h = sum(h.nbytes for _, h in self.host_out.values())
+        # The autotuner picks the temporal depth (sweeps per launch) for the
+        # iterated 2-D part; its records are used by the timed iterate calls.
+        self.tuned = {}
+        if "life" in self.parts:
+            d, rate = A.autotune_stencil2d(A.MSL_ST2_LIFE, A.MSL_I32, s, s, 1, 16)
+            self.tuned["life_temporal_depth"] = d
+            p = self.parts["life"]
+            p.launches = (self.life_steps + d - 1) // d
+            p.bytes_per_launch = 8 * s * s * self.life_steps // p.launches  # algorithmic, averaged over launches
 
     def updates(self):
         return sum(p.updates for p in self.parts.values())
@@ -354,6 +363,11 @@ class Jacobi:
         self.dev = {"jacobi": [A.DeviceArray.from_host(g), A.DeviceArray(g.shape, np.float32)]}
         self.h2d, self.d2h = h.nbytes, h.nbytes + 8
         self.residual = None
+        d, _ = A.autotune_stencil2d(A.MSL_ST2_JACOBI5, A.MSL_F32, self.side, self.side, 1, 64)
+        self.tuned = {"temporal_depth": d}
+        p = self.parts["jacobi"]
+        p.launches = (self.iters + d - 1) // d
+        p.bytes_per_launch = 8 * self.side * self.side * self.iters // p.launches
 
     def updates(self):
         return self.parts["jacobi"].updates
@@ -473,6 +487,96 @@ class MapZipFold:
         return self.bytes() / total_t / 1e9, f"2^25-element arrays ({threads} threads; folds on 1 thread)"
 
 
+class BatchSolve:
+    """Batched plain-Jacobi solves: 256 grids, sides log-uniform in [64, 2048]
+    rounded to multiples of 32 (seed 7), initialised as the plain-Jacobi grid
+    (per-grid seed 7000 + g), iterated to an FP64 residual <= 1e-4 (checked
+    every 100 sweeps) or the sweep cap. One step = one batched solve of all
+    grids from their initial values. Metric: solves per second."""
+    metric = "batched Jacobi solves/s"
+    unit = "solves/s"
+
+    def __init__(self, abi, count=256, storage="f32", cap=200_000, tol=1e-4, check_every=100, plain_sample=16):
+        self.A = abi
+        self.count, self.storage, self.cap, self.tol = count, storage, cap, tol
+        self.check_every, self.plain_sample = check_every, plain_sample
+        self.dtype = "f32" if storage == "f32" else "bf16-storage/f32-compute"
+        rng = np.random.default_rng(7)
+        u = rng.uniform(np.log(64), np.log(2048), count)
+        self.sides = [int(min(2048, max(64, round(np.exp(v) / 32) * 32))) for v in u]
+        self.parts = {}
+
+    def config(self):
+        return {"workload": f"{self.count} plain-Jacobi grids, sides log-uniform [64, 2048] (multiple of 32, seed 7), "
+                            f"{self.storage} storage, residual <= {self.tol} every {self.check_every} sweeps, "
+                            f"cap {self.cap} sweeps",
+                "cells": int(sum(n * n for n in self.sides))}
+
+    def setup(self):
+        from muesli4_gb300 import workloads as W
+        A = self.A
+        self.grids = [W.jacobi_grid(n, n, 7000 + g) for g, n in enumerate(self.sides)]
+        st = A.MSL_F32 if self.storage == "f32" else A.MSL_BF16
+        self.batch = A.Batch([(n, n) for n in self.sides], storage=st)
+        self.info = self.batch.info()
+        self.load_all()
+        self.depth, _ = A.autotune_stencil2d(A.MSL_ST2_JACOBI5, st, 1024, 1024, 1, 100)
+        while self.check_every % self.depth:
+            self.depth -= 1
+        self.tuned = {"temporal_depth": self.depth, "resident_grids": self.info["resident"],
+                      "worklist_tiles": self.info["tiles"]}
+        self.h2d = sum(g.nbytes for g in self.grids) // (1 if self.storage == "f32" else 2)
+        self.d2h = self.h2d
+
+    def updates(self):
+        return self.count
+
+    def load_all(self):
+        for i, g in enumerate(self.grids):
+            self.batch.set_grid(i, g)
+
+    def step(self, ev=None, marks=None):
+        self.batch.reset()  # initial values from their device copies
+        self.batch.solve(self.tol, self.cap, self.check_every, self.depth)
+
+    def e2e_step(self):
+        self.load_all()
+        self.batch.solve(self.tol, self.cap, self.check_every, self.depth)
+        out = []
+        for i in range(self.count):
+            out.append(self.batch.get_grid(i))
+        self.results = out
+
+    def summary(self):
+        res = [self.batch.get_grid(i) for i in range(self.count)]
+        iters = [r[1] for r in res]
+        conv = sum(1 for r in res if r[2] <= self.tol)
+        sweeps = sum(it * n * n for it, n in zip(iters, self.sides))
+        return res, {"converged": conv, "max_sweeps": int(max(iters)), "median_sweeps": float(np.median(iters)),
+                     "cell_updates": int(sweeps)}
+
+    def plain_rate(self):
+        """Solves/s of the one-grid-at-a-time path on a size-stratified sample."""
+        A = self.A
+        order = sorted(range(self.count), key=lambda g: self.sides[g])
+        sample = order[:: max(1, self.count // self.plain_sample)][: self.plain_sample]
+        st = np.float32 if self.storage == "f32" else np.uint16
+        t = 0.0
+        for g in sample:
+            from oracle import pyoracle as O
+            init = self.grids[g] if self.storage == "f32" else O.to_bf16(self.grids[g])
+            a, b = A.DeviceArray.from_host(init), A.DeviceArray(init.shape, st)
+            A.sync()
+            t0 = time.perf_counter()
+            A.solve_plain(A.MSL_ST2_JACOBI5, a, b, self.tol, self.cap, self.check_every)
+            A.sync()
+            t += time.perf_counter() - t0
+        return len(sample) / t, [self.sides[g] for g in sample]
+
+    def cpu_sample(self, O, threads, min_seconds: float = 0.0):
+        return None, "not measured"
+
+
 WORKLOADS = {
     "stencil_suite": lambda A: StencilSuite(A),
     "box": lambda A: StencilSuite(A, parts=("box",)),
@@ -480,6 +584,8 @@ WORKLOADS = {
     "heat": lambda A: StencilSuite(A, parts=("heat",)),
     "jacobi": lambda A: Jacobi(A),
     "mapzipfold": lambda A: MapZipFold(A),
+    "batch": lambda A: BatchSolve(A),
+    "batch_bf16": lambda A: BatchSolve(A, storage="bf16"),
 }
 
 
@@ -518,6 +624,74 @@ def run_reference(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, dist: Dist):
+    """Batched solves (BASELINE configs[3]): solves/s of the batched path, the
+    one-grid-at-a-time GPU path on a size-stratified sample, and the error of
+    a sample of results against FP64 sweeps computed by the CPU oracle."""
+    from muesli4_gb300 import abi as A
+    from oracle import pyoracle as O
+    A.init(dist.local_rank)
+    w = WORKLOADS[args.workload](A)
+    if args.batch_cap:
+        w.cap = max(w.check_every, args.batch_cap // w.check_every * w.check_every)
+    if args.batch_grids:
+        w.__init__(A, count=args.batch_grids, storage=w.storage, cap=w.cap)
+    w.setup()
+    ev = Events(A)
+    # Warm-up: short solves (a tenth of the cap) so that every kernel and the
+    # round graph have run before the timed solves.
+    for _ in range(args.warmup):
+        w.batch.reset()
+        w.batch.solve(w.tol, max(w.check_every, w.cap // 10 // w.check_every * w.check_every), w.check_every, w.depth)
+    A.sync()
+    dist.barrier()
+    sampler = ClockSampler(dist.local_rank)
+    sampler.start()
+    launches0 = A.launch_count()
+    e0 = ev.record()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        w.step()
+    e1 = ev.record()
+    A.sync()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    launches = A.launch_count() - launches0
+    dev_s = max(ev.ms(e0, e1) / 1e3, 1e-9)
+    t_max = dist.max(max(dev_s, wall))
+    value = dist.sum(w.count * args.steps) / t_max
+    results, summ = w.summary()
+    # end to end: host grids in, results out
+    t0 = time.perf_counter()
+    w.e2e_step()
+    A.sync()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    plain_rate, plain_sides = w.plain_rate()
+    # FP64 error of a sample of the smallest grids (CPU oracle, same sweep count)
+    errs = []
+    for g in sorted(range(w.count), key=lambda g: w.sides[g])[:4]:
+        got, it, _ = results[g]
+        init = w.grids[g].astype(np.float64)
+        ref = O.stencil2d_iterate(0, init, 1, 0.0, int(it))[0]
+        errs.append(float(np.max(np.abs(got.astype(np.float64) - ref))))
+    if dist.rank == 0:
+        gcups = summ["cell_updates"] / (t_max / args.steps) / 1e9
+        line = {
+            "metric": w.metric, "value": value, "unit": w.unit, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": w.dtype, "data": "synthetic",
+            "config": dict(w.config(), parallelism=f"replicas x{dist.world}", **w.tuned,
+                           warmup_note="warm-up solves use a tenth of the sweep cap"),
+            "e2e": {"value": w.count / e2e_s, "unit": w.unit, "h2d_bytes_per_step": w.h2d, "d2h_bytes_per_step": w.d2h},
+            "plain_path": {"value": plain_rate, "unit": w.unit, "sample_sides": plain_sides,
+                           "batched_over_plain": value / plain_rate},
+            "convergence": summ, "effective_GCUPS": gcups,
+            "max_error_vs_fp64_oracle": {"grids": "4 smallest, same sweep count", "max_abs": max(errs)},
+            "gpu_launches": launches, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -526,12 +700,19 @@ def main():
     ap.add_argument("--workload", default="stencil_suite", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-cap", type=int, default=0, help="sweep cap of the batch workloads")
+    ap.add_argument("--batch-grids", type=int, default=0, help="number of grids of the batch workloads")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     dist = Dist()
     if args.impl == "reference":
         run_reference(args, dist)
+        dist.close()
+        return
+
+    if args.workload.startswith("batch"):
+        run_batch(args, dist)
         dist.close()
         return
 
@@ -623,7 +804,7 @@ def main():
             "metric": w.metric, "value": value, "unit": w.unit, "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": w.dtype, "data": "synthetic",
-            "config": dict(w.config(), parallelism=f"replicas x{dist.world}"),
+            "config": dict(w.config(), parallelism=f"replicas x{dist.world}", **getattr(w, "tuned", {})),
             "e2e": {"value": e2e_value, "unit": w.unit, "h2d_bytes_per_step": w.h2d, "d2h_bytes_per_step": w.d2h},
             "roofline": {"bound": "hbm", "kernel": p.name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,

@@ -204,6 +204,32 @@ int msl_stencil3d(int dtype, int kind, const void *in, void *out, int depth, int
 int msl_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int rows, int cols,
                           int radius, double neutral, int iters, double *residual, int *result_in_b);
 
+/* ---- batched solves -----------------------------------------------------------
+ * Many independent plain-Jacobi grids (the MSL_ST2_JACOBI5 functor, radius 1)
+ * iterated together until each one's FP64 residual max |last - previous|,
+ * taken every `check_every` sweeps, is <= tol (or max_iters sweeps are done).
+ * Grids whose two iterates fit in one CTA's shared memory are solved there by
+ * one CTA each; the others share a tile work-list advanced by a persistent
+ * kernel, `depth` fused sweeps per round, the rounds replayed from a CUDA
+ * graph. Each grid's sweeps are exactly those of msl_stencil2d_iterate on that
+ * grid alone, so results do not depend on the rest of the batch.
+ * storage: MSL_F32, or MSL_BF16 (bfloat16 storage, FP32 arithmetic).
+ * hbm_budget (bytes, 0 = none): creation fails with MSL_ERR_BUDGET when the
+ * batch would need more device memory. No reference counterpart (the
+ * reference solves one DM at a time, examples/jacobisolver.cpp:110-145). */
+int msl_batch_create(int storage, int count, const int *rows, const int *cols, size_t hbm_budget, void **batch);
+/* Set grid `index` from FP32 host values (rounded to bfloat16 for BF16 storage). */
+int msl_batch_set_grid(void *batch, int index, const float *host_grid);
+/* Restore every grid to the values last given by msl_batch_set_grid (device copy). */
+int msl_batch_reset(void *batch);
+/* Iterate every grid; check_every must divide max_iters; depth 0 = autotuned. */
+int msl_batch_solve(void *batch, double tol, long long max_iters, int check_every, int depth);
+/* Latest iterate of grid `index` as FP32, with its sweep count and last residual. */
+int msl_batch_get_grid(void *batch, int index, float *host_out, long long *iters, double *residual);
+/* Grid count, grids solved CTA-resident, work-list tiles, device bytes (iterates and initial values). */
+int msl_batch_info(void *batch, int *count, int *resident, long long *tiles, size_t *device_bytes);
+int msl_batch_destroy(void *batch);
+
 /* ---- autotuner -------------------------------------------------------------
  * Times msl_stencil2d_iterate over `iters` sweeps of a rows x cols grid for
  * every temporal depth that fits (1, 2, 3, 4, 6, 8), on scratch grids it

@@ -71,6 +71,11 @@ def load() -> ctypes.CDLL:
         "msl_set_temporal_depth": [i], "msl_autotune_stencil2d": [i, i, i, i, i, i, ip, dp],
         "msl_autotune_save": [ctypes.c_char_p], "msl_autotune_load": [ctypes.c_char_p],
         "msl_fold_noalloc": [i, i, vp, sz, vp, vp],
+        "msl_batch_create": [i, i, ip, ip, sz, ctypes.POINTER(vp)], "msl_batch_set_grid": [vp, i, vp],
+        "msl_batch_solve": [vp, d, ctypes.c_longlong, i, i],
+        "msl_batch_get_grid": [vp, i, vp, ctypes.POINTER(ctypes.c_longlong), dp],
+        "msl_batch_info": [vp, ip, ip, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(sz)],
+        "msl_batch_destroy": [vp], "msl_batch_reset": [vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -135,6 +140,71 @@ def autotune_save(path: str) -> None:
 
 def autotune_load(path: str) -> None:
     check(load().msl_autotune_load(path.encode()), "msl_autotune_load")
+
+
+class Batch:
+    """Batched plain-Jacobi solves (msl_batch_*)."""
+
+    def __init__(self, shapes, storage=None, hbm_budget: int = 0):
+        self.shapes = [(int(r), int(c)) for r, c in shapes]
+        self.storage = MSL_F32 if storage is None else storage  # noqa: F821
+        rows = (ctypes.c_int * len(shapes))(*[r for r, _ in self.shapes])
+        cols = (ctypes.c_int * len(shapes))(*[c for _, c in self.shapes])
+        h = ctypes.c_void_p()
+        self.handle = None
+        check(load().msl_batch_create(self.storage, len(shapes), rows, cols, hbm_budget, ctypes.byref(h)),
+              "msl_batch_create")
+        self.handle = h
+
+    def set_grid(self, i: int, grid: np.ndarray) -> None:
+        g = np.ascontiguousarray(grid, dtype=np.float32)
+        assert g.shape == self.shapes[i]
+        check(load().msl_batch_set_grid(self.handle, i, g.ctypes.data), "msl_batch_set_grid")
+
+    def reset(self) -> None:
+        check(load().msl_batch_reset(self.handle), "msl_batch_reset")
+
+    def solve(self, tol: float, max_iters: int, check_every: int, depth: int = 0) -> None:
+        check(load().msl_batch_solve(self.handle, tol, max_iters, check_every, depth), "msl_batch_solve")
+
+    def get_grid(self, i: int):
+        out = np.empty(self.shapes[i], np.float32)
+        it, res = ctypes.c_longlong(), ctypes.c_double()
+        check(load().msl_batch_get_grid(self.handle, i, out.ctypes.data, ctypes.byref(it), ctypes.byref(res)),
+              "msl_batch_get_grid")
+        return out, it.value, res.value
+
+    def info(self):
+        n, res, tiles, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong(), ctypes.c_size_t()
+        check(load().msl_batch_info(self.handle, ctypes.byref(n), ctypes.byref(res), ctypes.byref(tiles),
+                                    ctypes.byref(b)), "msl_batch_info")
+        return {"count": n.value, "resident": res.value, "tiles": tiles.value, "device_bytes": b.value}
+
+    def close(self) -> None:
+        if self.handle:
+            load().msl_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_plain(kind: int, grid: DeviceArray, other: DeviceArray, tol: float, max_iters: int, check_every: int):
+    """One grid at a time: msl_stencil2d_iterate in chunks of check_every sweeps
+    until the residual is <= tol. Returns (array holding the result, sweeps, residual)."""
+    a, b = grid, other
+    it, res = 0, float("inf")
+    while it < max_iters:
+        last, res = stencil2d_iterate(kind, a, b, 1, 0.0, check_every)
+        it += check_every
+        if last is b:
+            a, b = b, a
+        if not res > tol:
+            break
+    return a, it, res
 
 
 def device_info():

@@ -1,0 +1,327 @@
+// Batched plain-Jacobi solver of libmsl_gb300.so (msl_batch_*): many grids of
+// uneven size iterated to an FP64 residual tolerance together. See
+// include/detail/msl_batch.cuh for the kernels.
+//
+// No reference counterpart: the reference solves one DM at a time
+// (examples/jacobisolver.cpp:110-145).
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "../include/detail/msl_batch.cuh"
+#include "msl_internal.h"
+
+using namespace msl;
+using namespace msl::gpu;
+using msl::rt::ctx;
+
+namespace {
+
+constexpr size_t kResidentSmemMax = 200 * 1024;  // both iterates of a resident grid
+
+struct Batch {
+    int storage = MSL_F32;
+    size_t es = 4;
+    std::vector<int> rows, cols;
+    void *pool = nullptr;
+    size_t pool_bytes = 0;
+    std::vector<BatchGrid> host;
+    std::vector<void *> init;  // initial values of each grid (msl_batch_reset restores them)
+    BatchGrid *dev = nullptr;
+    int *d_lists = nullptr;  // resident list | work list
+    int *d_active = nullptr;
+    int *h_active = nullptr;  // pinned
+    std::vector<int> resident, worklist;
+    long long total_tiles = 0;
+    size_t resident_smem = 0;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+size_t grid_bytes(const Batch &b, int i) { return ((size_t)b.rows[i] * b.cols[i] * b.es + 255) / 256 * 256; }
+size_t resident_need(const Batch &b, int i) {
+    const size_t n = (size_t)b.rows[i] * b.cols[i];
+    return 2 * ((n * b.es + 127) / 128 * 128);
+}
+
+template <typename S> size_t round_smem(int depth) { return stencil2d_tb_smem<S>(1, depth); }
+
+void destroy(Batch *b) {
+    if (!b) return;
+    if (b->pool) cudaFree(b->pool);
+    if (b->dev) cudaFree(b->dev);
+    if (b->d_lists) cudaFree(b->d_lists);
+    if (b->d_active) cudaFree(b->d_active);
+    if (b->h_active) cudaFreeHost(b->h_active);
+    if (b->side) cudaStreamDestroy(b->side);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
+    delete b;
+}
+
+float bf16_bits_to_f(uint16_t h) {
+    uint32_t u = (uint32_t)h << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+uint16_t f_to_bf16_bits(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40u);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+template <typename S>
+int solve_t(Batch &b, double tol, long long max_iters, int check_every, int depth) {
+    auto &c = ctx();
+    cudaStream_t st = c.stream;
+    // Reset the solve state of every grid (the data stay).
+    for (auto &g : b.host) {
+        g.done = 0;
+        g.iters = 0;
+        g.residual = 0.0;
+        g.resid_bits = 0ull;
+    }
+    MSL_TRY_CUDA(cudaMemcpyAsync(b.dev, b.host.data(), b.host.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice, st),
+                 "msl_batch_solve");
+    // Resident grids: one launch on the side stream, overlapping the rounds.
+    if (!b.resident.empty()) {
+        MSL_TRY_CUDA(cudaEventRecord(b.fork, st), "msl_batch_solve");
+        MSL_TRY_CUDA(cudaStreamWaitEvent(b.side, b.fork, 0), "msl_batch_solve");
+        auto k = batch_resident_kernel<S>;
+        MSL_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b.resident_smem),
+                     "msl_batch_solve");
+        k<<<(unsigned)b.resident.size(), kBatchResidentThreads, b.resident_smem, b.side>>>(b.dev, b.d_lists, tol, max_iters,
+                                                                                           check_every);
+        MSL_TRY_CUDA(cudaGetLastError(), "msl_batch_solve: resident kernel");
+        rt::count_launch();
+        MSL_TRY_CUDA(cudaEventRecord(b.join, b.side), "msl_batch_solve");
+    }
+    if (!b.worklist.empty()) {
+        const int nlist = (int)b.worklist.size();
+        const int *wl = b.d_lists + b.resident.size();
+        const size_t smem = round_smem<S>(depth);
+        auto rk = batch_round_kernel<S>;
+        if (smem > 48 * 1024)
+            MSL_TRY_CUDA(cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "msl_batch_solve");
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rk, kSt2Threads, smem);
+        const long long grid = std::max(1LL, std::min<long long>(b.total_tiles, (long long)std::max(per_sm, 1) * c.sm_count));
+        // Rounds per graph: even (parity returns to 0) and a whole number of check chunks.
+        const int chunk_rounds = check_every / depth;
+        int rounds = chunk_rounds % 2 ? 2 * chunk_rounds : chunk_rounds;
+        while (rounds < 8) rounds *= 2;
+        cudaGraph_t graph;
+        cudaGraphExec_t exec;
+        MSL_TRY_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "msl_batch_solve: capture");
+        for (int j = 0; j < rounds; j++) {
+            const int check = ((j + 1) % chunk_rounds) == 0;
+            rk<<<(unsigned)grid, kSt2Threads, smem, st>>>(b.dev, wl, nlist, b.total_tiles, j & 1, depth, check);
+            batch_finalize_kernel<<<1, 256, 0, st>>>(b.dev, wl, nlist, depth, (j + 1) & 1, check, tol, max_iters,
+                                                      b.d_active);
+        }
+        cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        if (ce != cudaSuccess) return rt::cuda_fail(ce, "msl_batch_solve: capture");
+        ce = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return rt::cuda_fail(ce, "msl_batch_solve: instantiate");
+        const long long max_replays = max_iters / ((long long)rounds * depth) + 2;
+        int rc = MSL_OK;
+        for (long long rep = 0; rep < max_replays; rep++) {
+            ce = cudaGraphLaunch(exec, st);
+            if (ce == cudaSuccess) ce = cudaMemcpyAsync(b.h_active, b.d_active, sizeof(int), cudaMemcpyDeviceToHost, st);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+            if (ce != cudaSuccess) {
+                rc = rt::cuda_fail(ce, "msl_batch_solve: rounds");
+                break;
+            }
+            rt::count_launch(2 * rounds);
+            if (*(volatile int *)b.h_active == 0) break;
+        }
+        cudaGraphExecDestroy(exec);
+        if (rc != MSL_OK) return rc;
+    }
+    if (!b.resident.empty()) MSL_TRY_CUDA(cudaStreamWaitEvent(st, b.join, 0), "msl_batch_solve");
+    MSL_TRY_CUDA(cudaMemcpyAsync(b.host.data(), b.dev, b.host.size() * sizeof(BatchGrid), cudaMemcpyDeviceToHost, st),
+                 "msl_batch_solve");
+    MSL_TRY_CUDA(cudaStreamSynchronize(st), "msl_batch_solve");
+    return rt::check_device_errors("msl_batch_solve");
+}
+
+}  // namespace
+
+extern "C" {
+
+int msl_batch_create(int storage, int count, const int *rows, const int *cols, size_t hbm_budget, void **batch) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    if (int e = rt::require_init()) return e;
+    if (!batch || !rows || !cols || count <= 0)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_create: bad arguments");
+    if (storage != MSL_F32 && storage != MSL_BF16)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_create: storage must be MSL_F32 or MSL_BF16");
+    *batch = nullptr;
+    Batch *b = new Batch;
+    b->storage = storage;
+    b->es = rt::dtype_size(storage);
+    b->rows.assign(rows, rows + count);
+    b->cols.assign(cols, cols + count);
+    for (int i = 0; i < count; i++) {
+        if (rows[i] < 1 || cols[i] < 1 || (long long)rows[i] * cols[i] > (1LL << 30)) {
+            destroy(b);
+            return rt::fail(MSL_ERR_SIZE_MISMATCH, "msl_batch_create: grid %d is %d x %d", i, rows[i], cols[i]);
+        }
+        b->pool_bytes += 3 * grid_bytes(*b, i);
+    }
+    const size_t meta = count * sizeof(BatchGrid) + 2 * count * sizeof(int) + 64;
+    if (hbm_budget && b->pool_bytes + meta > hbm_budget) {
+        size_t need = b->pool_bytes + meta;
+        destroy(b);
+        return rt::fail(MSL_ERR_BUDGET, "msl_batch_create: %zu bytes needed, budget %zu", need, hbm_budget);
+    }
+    cudaError_t e = cudaMalloc(&b->pool, b->pool_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&b->dev, count * sizeof(BatchGrid));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_lists, 2 * count * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_active, sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_active, sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        destroy(b);
+        return rt::cuda_fail(e, "msl_batch_create");
+    }
+    char *p = (char *)b->pool;
+    b->host.resize(count);
+    b->init.resize(count);
+    for (int i = 0; i < count; i++) {
+        BatchGrid &gd = b->host[i];
+        memset(&gd, 0, sizeof gd);
+        gd.rows = rows[i];
+        gd.cols = cols[i];
+        gd.buf[0] = p;
+        p += grid_bytes(*b, i);
+        gd.buf[1] = p;
+        p += grid_bytes(*b, i);
+        b->init[i] = p;
+        p += grid_bytes(*b, i);
+        if (resident_need(*b, i) <= kResidentSmemMax) {
+            b->resident.push_back(i);
+            b->resident_smem = std::max(b->resident_smem, resident_need(*b, i));
+        } else {
+            b->worklist.push_back(i);
+        }
+    }
+    // Work-list tile prefix (64 x 32 tiles).
+    for (int i : b->worklist) {
+        b->host[i].first_tile = b->total_tiles;
+        b->total_tiles += (long long)((cols[i] + kSt2BX - 1) / kSt2BX) * ((rows[i] + kSt2BY - 1) / kSt2BY);
+    }
+    std::vector<int> lists(b->resident);
+    lists.insert(lists.end(), b->worklist.begin(), b->worklist.end());
+    e = cudaMemcpy(b->d_lists, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->pool, 0, b->pool_bytes);
+    if (e != cudaSuccess) {
+        destroy(b);
+        return rt::cuda_fail(e, "msl_batch_create");
+    }
+    *batch = b;
+    return MSL_OK;
+}
+
+int msl_batch_destroy(void *batch) {
+    std::lock_guard<std::recursive_mutex> g(ctx().mu);
+    if (batch) {
+        cudaStreamSynchronize(ctx().stream);
+        destroy((Batch *)batch);
+    }
+    return MSL_OK;
+}
+
+int msl_batch_set_grid(void *batch, int index, const float *host_grid) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    Batch *b = (Batch *)batch;
+    if (!b || !host_grid || index < 0 || index >= (int)b->host.size())
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_set_grid: bad arguments");
+    const size_t n = (size_t)b->rows[index] * b->cols[index];
+    BatchGrid &gd = b->host[index];
+    gd.cur = 0;
+    if (b->storage == MSL_F32) {
+        MSL_TRY_CUDA(cudaMemcpy(gd.buf[0], host_grid, n * 4, cudaMemcpyHostToDevice), "msl_batch_set_grid");
+    } else {
+        std::vector<uint16_t> h(n);
+        for (size_t i = 0; i < n; i++) h[i] = f_to_bf16_bits(host_grid[i]);
+        MSL_TRY_CUDA(cudaMemcpy(gd.buf[0], h.data(), n * 2, cudaMemcpyHostToDevice), "msl_batch_set_grid");
+    }
+    MSL_TRY_CUDA(cudaMemcpy(b->init[index], gd.buf[0], n * b->es, cudaMemcpyDeviceToDevice), "msl_batch_set_grid");
+    return MSL_OK;
+}
+
+int msl_batch_get_grid(void *batch, int index, float *host_out, long long *iters, double *residual) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    Batch *b = (Batch *)batch;
+    if (!b || !host_out || index < 0 || index >= (int)b->host.size())
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_get_grid: bad arguments");
+    MSL_TRY_CUDA(cudaStreamSynchronize(c.stream), "msl_batch_get_grid");
+    const size_t n = (size_t)b->rows[index] * b->cols[index];
+    const BatchGrid &gd = b->host[index];
+    if (b->storage == MSL_F32) {
+        MSL_TRY_CUDA(cudaMemcpy(host_out, gd.buf[gd.cur], n * 4, cudaMemcpyDeviceToHost), "msl_batch_get_grid");
+    } else {
+        std::vector<uint16_t> h(n);
+        MSL_TRY_CUDA(cudaMemcpy(h.data(), gd.buf[gd.cur], n * 2, cudaMemcpyDeviceToHost), "msl_batch_get_grid");
+        for (size_t i = 0; i < n; i++) host_out[i] = bf16_bits_to_f(h[i]);
+    }
+    if (iters) *iters = gd.iters;
+    if (residual) *residual = gd.residual;
+    return MSL_OK;
+}
+
+int msl_batch_solve(void *batch, double tol, long long max_iters, int check_every, int depth) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    if (int e = rt::require_init()) return e;
+    Batch *b = (Batch *)batch;
+    if (!b) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_solve: NULL batch");
+    if (check_every < 1 || max_iters < 1 || max_iters % check_every)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT,
+                        "msl_batch_solve: check_every must be >= 1 and divide max_iters (%lld, %d)", max_iters,
+                        check_every);
+    if (depth <= 0) depth = rt::tuned_depth(b->storage, MSL_ST2_JACOBI5, 1024, 1024, 1);
+    while (depth > 1 && check_every % depth) depth--;
+    if (depth > 8) depth = 8;
+    return b->storage == MSL_F32 ? solve_t<float>(*b, tol, max_iters, check_every, depth)
+                                 : solve_t<bf16s>(*b, tol, max_iters, check_every, depth);
+}
+
+int msl_batch_reset(void *batch) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    Batch *b = (Batch *)batch;
+    if (!b) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_reset: NULL batch");
+    for (size_t i = 0; i < b->host.size(); i++) {
+        const size_t n = (size_t)b->rows[i] * b->cols[i];
+        MSL_TRY_CUDA(cudaMemcpyAsync(b->host[i].buf[0], b->init[i], n * b->es, cudaMemcpyDeviceToDevice, c.stream),
+                     "msl_batch_reset");
+        b->host[i].cur = 0;
+    }
+    return MSL_OK;
+}
+
+int msl_batch_info(void *batch, int *count, int *resident, long long *tiles, size_t *device_bytes) {
+    Batch *b = (Batch *)batch;
+    if (!b) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_info: NULL batch");
+    if (count) *count = (int)b->host.size();
+    if (resident) *resident = (int)b->resident.size();
+    if (tiles) *tiles = b->total_tiles;
+    if (device_bytes) *device_bytes = b->pool_bytes;
+    return MSL_OK;
+}
+
+}  // extern "C"

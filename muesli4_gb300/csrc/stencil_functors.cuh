@@ -107,7 +107,8 @@ template <typename T> struct StHeat7 {
         v = Arith<T>::add(v, c(x, y + 1, z));
         v = Arith<T>::add(v, c(x, y, z - 1));
         v = Arith<T>::add(v, c(x, y, z + 1));
-        return div_rn<T>(v, T(6));
+        if constexpr (std::is_same<T, float>::value) return div6_rn(v);  // == v / 6, correctly rounded
+        else return div_rn<T>(v, T(6));
     }
 };
 // 3-D box, dx outer, dy, dz inner (examples/meanblur2.cpp:46-57).

@@ -207,3 +207,27 @@ template <typename T> MSL_DEV T shfl_down(T v, int delta) {
 
 }  // namespace gpu
 }  // namespace msl
+
+namespace msl {
+namespace gpu {
+
+// x / 6 rounded to nearest, via the reciprocal-with-one-correction method for
+// a divisor known in advance (P. Markstein, "IA-64 and Elementary Functions",
+// 2000; N. Brisebarre, J.-M. Muller, S. K. Raina, "Accelerating correctly
+// rounded floating-point division when the divisor is known in advance",
+// IEEE Trans. Computers 53(8), 2004): q = RN(x * RN(1/6)), remainder
+// r = x - 6q exactly by one FMA, then q' = RN(q + r * RN(1/6)). The result is
+// checked against IEEE division for every one of the 2^32 float inputs by the
+// GPU test suite. The method needs a normal quotient, so inputs below 2^-122
+// in magnitude take IEEE division; infinities and NaNs pass through q.
+MSL_DEV float div6_rn(float x) {
+    if (fabsf(x) < 1.88079096131566e-37f) return __fdiv_rn(x, 6.0f);  // 2^-122
+    const float zh = 0.16666667163372039794921875f;  // RN(1/6)
+    const float q = __fmul_rn(x, zh);
+    const float r = __fmaf_rn(-q, 6.0f, x);
+    const float q2 = __fmaf_rn(r, zh, q);
+    return isfinite(q) ? q2 : q;
+}
+
+}  // namespace gpu
+}  // namespace msl

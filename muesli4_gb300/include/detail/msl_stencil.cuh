@@ -76,10 +76,11 @@ template <typename T, typename S = T> class PLCube {
     int width = 0, height = 0, depth = 0;
     int stencilSize = 0;
     T neutralValue{};
-    // ring of planes: plane z lives in slot (z & mask_) while zlo_ <= z <= zhi_
+    // ring of planes: plane z lives in slot (z & mask_) - oz_ while zlo_ <= z <= zhi_
     const S *ring_ = nullptr;
     const S *global_ = nullptr;
     int ox_ = 0, oy_ = 0, pitch_ = 0, tile_h_ = 0, plane_ = 0, mask_ = 0, zlo_ = 0, zhi_ = -1;
+    int oz_ = 0;  // plane index of slot 0 when the planes form a linear box (mask_ = -1)
     bool check_ = true;
 
     __host__ __device__ __forceinline__ T operator()(int x, int y, int z) const {
@@ -93,7 +94,7 @@ template <typename T, typename S = T> class PLCube {
 #endif
         if (check_ && ((unsigned)x >= (unsigned)width || (unsigned)y >= (unsigned)height || (unsigned)z >= (unsigned)depth))
             return neutralValue;
-        return gpu::widen<S>(ring_[(z & mask_) * plane_ + (y - oy_) * pitch_ + (x - ox_)]);
+        return gpu::widen<S>(ring_[((z & mask_) - oz_) * plane_ + (y - oy_) * pitch_ + (x - ox_)]);
     }
 };
 
@@ -365,19 +366,17 @@ MSL_DEV void stencil3d_strip(const Fn &fn, const View &c, int x, int ys, int z, 
         if (FULL || ys + j < rows) o[(size_t)j * cols] = narrow<S>(vals[j]);
 }
 
-// Persistent 3-D kernel. The cube is cut into 64 x 32 (x, y) tiles; the
-// tile-planes (tile, z) are numbered tile-major and every CTA takes an equal
-// contiguous range of them, so all CTAs are resident and finish together
-// (no partial last wave). A range is one or more z-segments of tiles; each
-// segment is a z-march with a ring of NS = 2^k >= 2r+2 shared-memory planes,
-// one TMA 3-D load per plane issued one plane ahead, one mbarrier per slot
-// (its phase tracked in a bit mask). Only the first 2r planes of a segment are
-// re-read halo.
+// 3-D kernel. The cube is cut into 64 x 32 (x, y) tiles and each tile's
+// depth into z-chunks; one CTA per (tile, chunk), sized so that all CTAs are
+// resident together. Each CTA's work is a z-march with a ring of
+// NS = 2^k >= 2r+2 shared-memory planes, one TMA 3-D load per plane issued one
+// plane ahead, one mbarrier per slot (its phase tracked in a bit mask). Only
+// the first 2r planes of a chunk are re-read halo.
 template <typename S, class Fn, bool TMA>
-__global__ void __launch_bounds__(kSt3Threads)
+__global__ void __launch_bounds__(kSt3Threads, 5)
     stencil3d_kernel(const __grid_constant__ CUtensorMap tmap, const S *in, S *out, int depth, int rows, int cols,
-                     int r, int hx, int ns_log2, typename Compute<S>::type neutral, Fn fn, unsigned long long *resid,
-                     unsigned *err) {
+                     int r, int hx, int ns_log2, int zchunk, typename Compute<S>::type neutral, Fn fn,
+                     unsigned long long *resid, unsigned *err) {
     using T = typename Compute<S>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw);  // up to 16 slots
@@ -387,8 +386,13 @@ __global__ void __launch_bounds__(kSt3Threads)
     const int plane = (pitch * th + 31) / 32 * 32;  // keeps every slot 128-byte aligned
     const uint32_t plane_bytes = (uint32_t)(pitch * th * sizeof(S));
     const int tiles_x = (cols + kSt3BX - 1) / kSt3BX, tiles_y = (rows + kSt3BY - 1) / kSt3BY;
-    const long long total = (long long)tiles_x * tiles_y * depth;
-    const long long begin = total * blockIdx.x / gridDim.x, end = total * (blockIdx.x + 1) / gridDim.x;
+    // CTA b marches tile (b mod tiles) through z-chunk (b / tiles): adjacent
+    // tiles run side by side at the same depth, so the halo lines one CTA
+    // fetches are still in L2 when its neighbours need them.
+    const int tiles = tiles_x * tiles_y;
+    const int tile0 = (int)(blockIdx.x % tiles), zc = (int)(blockIdx.x / tiles);
+    const int zlo = zc * zchunk, zhi = min(depth, zlo + zchunk);
+    const long long begin = (long long)tile0 * depth + zlo, end = (long long)tile0 * depth + max(zlo, zhi);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool want = resid != nullptr;
     double dmax = 0.0;
@@ -485,6 +489,115 @@ __global__ void __launch_bounds__(kSt3Threads)
     }
     if (want) {
         __syncthreads();
+        dmax = block_max(dmax);
+        if (threadIdx.x == 0) atomic_max_nonneg(resid, dmax);
+    }
+}
+
+// 3-D tile kernel: one CTA per 64 x 16 x 8 block of outputs, staged with a
+// single TMA 3-D load of the block plus its halo (the same design as the 2-D
+// kernel: no per-plane synchronisation, many CTAs in flight, neighbouring
+// blocks launched next to each other so halos are served from L2). Each
+// thread computes a 4-row x 8-plane strip of one column, all values before any
+// store. Used for radius <= kT3MaxR; larger radii use the z-march kernel.
+constexpr int kT3BX = 64, kT3BY = 16, kT3BZ = 8, kT3RPT = 4, kT3Threads = 256, kT3MaxR = 3;
+
+template <typename S, bool FULL, class Fn, class View>
+MSL_DEV void stencil3d_block(const Fn &fn, const View &c, int x, int ys, int z0, int depth, int rows, int cols, S *out,
+                             bool want, double &dmax) {
+    using T = typename Compute<S>::type;
+    if (!FULL && x >= cols) return;
+#pragma unroll
+    for (int k = 0; k < kT3BZ; k++) {
+        const int z = z0 + k;
+        if (!FULL && z >= depth) break;
+        T vals[kT3RPT];
+#pragma unroll
+        for (int j = 0; j < kT3RPT; j++)
+            if (FULL || ys + j < rows) vals[j] = fn(c, x, ys + j, z);
+        if (want) {
+#pragma unroll
+            for (int j = 0; j < kT3RPT; j++)
+                if (FULL || ys + j < rows) {
+                    const double d = fabs(stored_f64(narrow<S>(vals[j])) - (double)c(x, ys + j, z));
+                    if (d > dmax || d != d) dmax = d;
+                }
+        }
+        S *o = out + ((size_t)z * rows + ys) * cols + x;
+#pragma unroll
+        for (int j = 0; j < kT3RPT; j++)
+            if (FULL || ys + j < rows) o[(size_t)j * cols] = narrow<S>(vals[j]);
+    }
+}
+
+template <typename S, class Fn, bool TMA>
+__global__ void __launch_bounds__(kT3Threads, 3)
+    stencil3d_tile_kernel(const __grid_constant__ CUtensorMap tmap, const S *in, S *out, int depth, int rows,
+                          int cols, int r, int hx, typename Compute<S>::type neutral, Fn fn,
+                          unsigned long long *resid, unsigned *err) {
+    using T = typename Compute<S>::type;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
+    S *box = reinterpret_cast<S *>(smem_raw + kStHeader);
+    const int pitch = kT3BX + 2 * hx, th = kT3BY + 2 * r, tz = kT3BZ + 2 * r;
+    const int x0 = blockIdx.x * kT3BX, y0 = blockIdx.y * kT3BY, z0 = blockIdx.z * kT3BZ;
+    const int wx0 = x0 - hx, wy0 = y0 - r, wz0 = z0 - r;
+    bool ok = true;
+    if constexpr (TMA) {
+        if (threadIdx.x == 0) {
+            mbar_init(bar, 1);
+            fence_barrier_init();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_arrive_expect_tx(bar, (uint32_t)(pitch * th * tz * sizeof(S)));
+            tma_load_3d(box, &tmap, bar, wx0, wy0, wz0);
+        }
+        ok = mbar_wait_bounded(bar, 0, err);
+    } else {
+        for (int i = threadIdx.x; i < pitch * th * tz; i += blockDim.x) {
+            const int zz = i / (pitch * th), rem = i - zz * pitch * th, yy = rem / pitch, xx = rem - yy * pitch;
+            const int gx = wx0 + xx, gy = wy0 + yy, gz = wz0 + zz;
+            box[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows && gz >= 0 && gz < depth)
+                         ? in[((size_t)gz * rows + gy) * cols + gx]
+                         : S{};
+        }
+    }
+    ok = __syncthreads_and(ok);
+    if (!ok) return;
+
+    PLCube<T, S> c;
+    c.width = cols;
+    c.height = rows;
+    c.depth = depth;
+    c.stencilSize = r;
+    c.neutralValue = neutral;
+    c.ring_ = box;
+    c.global_ = in;
+    c.ox_ = wx0;
+    c.oy_ = wy0;
+    c.oz_ = wz0;
+    c.pitch_ = pitch;
+    c.tile_h_ = th;
+    c.plane_ = pitch * th;
+    c.mask_ = -1;
+    c.zlo_ = wz0;
+    c.zhi_ = wz0 + tz - 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x = x0 + (warp % (kT3BX / 32)) * 32 + lane;
+    const int ys = y0 + (warp / (kT3BX / 32)) * kT3RPT;
+    const bool interior = wx0 >= 0 && wy0 >= 0 && wz0 >= 0 && wx0 + pitch <= cols && wy0 + th <= rows &&
+                          wz0 + tz <= depth;
+    const bool want = resid != nullptr;
+    double dmax = 0.0;
+    if (interior) {
+        c.check_ = false;
+        stencil3d_block<S, true>(fn, c, x, ys, z0, depth, rows, cols, out, want, dmax);
+    } else {
+        c.check_ = true;
+        stencil3d_block<S, false>(fn, c, x, ys, z0, depth, rows, cols, out, want, dmax);
+    }
+    if (want) {
         dmax = block_max(dmax);
         if (threadIdx.x == 0) atomic_max_nonneg(resid, dmax);
     }
@@ -606,10 +719,43 @@ cudaError_t launch_stencil2d_tb(const S *in, S *out, int rows, int cols, int r, 
     return cudaGetLastError();
 }
 
+template <typename S> inline size_t stencil3d_tile_smem(int r) {
+    return (size_t)kStHeader +
+           (size_t)(kT3BX + 2 * halo_x<S>(r)) * (kT3BY + 2 * r) * (kT3BZ + 2 * r) * sizeof(S);
+}
+
+template <typename S, class Fn>
+cudaError_t launch_stencil3d_tile(const S *in, S *out, int depth, int rows, int cols, int r,
+                                  typename Compute<S>::type neutral, Fn fn, unsigned long long *resid, unsigned *err,
+                                  cudaStream_t st, bool allow_tma) {
+    const int hx = halo_x<S>(r);
+    const int pitch = kT3BX + 2 * hx, th = kT3BY + 2 * r, tz = kT3BZ + 2 * r;
+    const size_t smem = stencil3d_tile_smem<S>(r);
+    dim3 grid((cols + kT3BX - 1) / kT3BX, (rows + kT3BY - 1) / kT3BY, (depth + kT3BZ - 1) / kT3BZ);
+    CUtensorMap map{};
+    const bool tma = allow_tma && stencil_tma_ok<S>(in, cols, pitch, th) && tz <= 256;
+    auto k = tma ? stencil3d_tile_kernel<S, Fn, true> : stencil3d_tile_kernel<S, Fn, false>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (tma) {
+        cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)depth};
+        cuuint64_t strides[2] = {(cuuint64_t)cols * sizeof(S), (cuuint64_t)cols * rows * sizeof(S)};
+        cuuint32_t box[3] = {(cuuint32_t)pitch, (cuuint32_t)th, (cuuint32_t)tz};
+        cuuint32_t estr[3] = {1, 1, 1};
+        if (tensor_map_encoder()(&map, tmap_dtype<S>(), 3, const_cast<S *>(in), dims, strides, box, estr,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+    }
+    k<<<grid, kT3Threads, smem, st>>>(map, in, out, depth, rows, cols, r, hx, neutral, fn, resid, err);
+    return cudaGetLastError();
+}
+
 template <typename S, class Fn>
 cudaError_t launch_stencil3d(const S *in, S *out, int depth, int rows, int cols, int r,
                              typename Compute<S>::type neutral, Fn fn, unsigned long long *resid, unsigned *err,
                              cudaStream_t st, int sm_count, bool allow_tma = true) {
+    if (r <= kT3MaxR && stencil3d_tile_smem<S>(r) <= 120 * 1024)
+        return launch_stencil3d_tile<S>(in, out, depth, rows, cols, r, neutral, fn, resid, err, st, allow_tma);
     const int hx = halo_x<S>(r);
     const int pitch = kSt3BX + 2 * hx, th = kSt3BY + 2 * r;
     const int ns_log2 = st3_ns_log2(r);
@@ -625,10 +771,16 @@ cudaError_t launch_stencil3d(const S *in, S *out, int depth, int rows, int cols,
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kSt3Threads, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
-    long long grid = (long long)per_sm * (sm_count > 0 ? sm_count : 152);
-    const long long by_work = (total + 7) / 8;
-    if (grid > by_work) grid = by_work;
-    if (grid < 1) grid = 1;
+    // As many z-chunks per tile as the resident CTA slots allow (chunks of at
+    // least 8 planes); one chunk per tile when the cross-section alone fills the GPU.
+    const long long tiles = total / depth;
+    const long long slots = (long long)per_sm * (sm_count > 0 ? sm_count : 152);
+    long long nz = slots / tiles;
+    if (nz > depth / 8) nz = depth / 8;
+    if (nz < 1) nz = 1;
+    const int zchunk = (int)((depth + nz - 1) / nz);
+    nz = (depth + zchunk - 1) / zchunk;
+    const long long grid = tiles * nz;
     if (tma) {
         cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)depth};
         cuuint64_t strides[2] = {(cuuint64_t)cols * sizeof(S), (cuuint64_t)cols * rows * sizeof(S)};
@@ -639,8 +791,8 @@ cudaError_t launch_stencil3d(const S *in, S *out, int depth, int rows, int cols,
                                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return cudaErrorInvalidValue;
     }
-    k<<<(unsigned)grid, kSt3Threads, smem, st>>>(map, in, out, depth, rows, cols, r, hx, ns_log2, neutral, fn, resid,
-                                                 err);
+    k<<<(unsigned)grid, kSt3Threads, smem, st>>>(map, in, out, depth, rows, cols, r, hx, ns_log2, zchunk, neutral, fn,
+                                                 resid, err);
     return cudaGetLastError();
 }
 
