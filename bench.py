@@ -624,6 +624,108 @@ def run_reference(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+def serve_requests(count: int, seed: int = 11):
+    """Request stream of the served-solves workload: half 2-D plain-Jacobi
+    grids n x n with n log-uniform in [64, 4096], half 3-D heat cubes m^3 with
+    m log-uniform in [32, 256]; U[0,1) initial values from a per-request seed."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        if rng.random() < 0.5:
+            n = int(round(np.exp(rng.uniform(np.log(64), np.log(4096)))))
+            reqs.append(("2d", (n, n), seed * 100000 + i))
+        else:
+            m = int(round(np.exp(rng.uniform(np.log(32), np.log(256)))))
+            reqs.append(("3d", (m, m, m), seed * 100000 + i))
+    return reqs
+
+
+def run_serve(args, dist: Dist):
+    """Served stencil solves (BASELINE configs[4]): Poisson arrivals at rates
+    swept around the plain path's capacity; p50/p99 latency and solves/s of the
+    continuously batching server against the one-request-at-a-time GPU path
+    (FIFO queue fed the same arrivals; its service times are measured on a
+    sample of the requests and the queue is replayed from them)."""
+    from muesli4_gb300 import abi as A
+    A.init(dist.local_rank)
+    tol, cap, check = 1e-4, 5000, 100
+    reqs = serve_requests(args.serve_requests)
+    cache = {}
+
+    def init_of(i):
+        if i not in cache:
+            kind, shape, sd = reqs[i]
+            cache[i] = np.random.default_rng(sd).random(shape, dtype=np.float32)
+        return cache[i]
+
+    # plain path: service time of a sample of requests, one at a time
+    rng = np.random.default_rng(5)
+    sample = sorted(rng.choice(len(reqs), size=min(args.serve_plain_sample, len(reqs)), replace=False).tolist())
+    service = []
+    for i in sample:
+        x = init_of(i)
+        kind = A.MSL_ST3_HEAT7 if x.ndim == 3 else A.MSL_ST2_JACOBI5
+        a, b = A.DeviceArray.from_host(x), A.DeviceArray(x.shape, np.float32)
+        A.sync()
+        t0 = time.perf_counter()
+        out, _, _ = A.solve_plain(kind, a, b, tol, cap, check)
+        out.download()
+        service.append(time.perf_counter() - t0)
+    plain_capacity = len(service) / sum(service)
+
+    def plain_queue(arrivals):
+        """FIFO replay of the plain path with service times drawn from the sample."""
+        r = np.random.default_rng(9)
+        t_free, lat = 0.0, []
+        for a in arrivals:
+            start = max(a, t_free)
+            t_free = start + service[int(r.integers(len(service)))]
+            lat.append(t_free - a)
+        return len(arrivals) / (t_free - arrivals[0]), lat
+
+    sweep = []
+    for factor in args.serve_rates:
+        lam = factor * plain_capacity
+        arr = np.cumsum(np.random.default_rng(11).exponential(1.0 / lam, len(reqs)))
+        arr -= arr[0]
+        srv = A.Server(hbm_budget=120 << 30, tol=tol, max_iters=cap, check_every=check)
+        t0 = time.perf_counter()
+        ids = []
+        for i, a in enumerate(arr):
+            now = time.perf_counter() - t0
+            if a > now:
+                time.sleep(a - now)
+            ids.append(srv.submit(init_of(i)))
+        lat, queued, sweeps = [], [], 0
+        for rid in ids:
+            srv.wait(rid, -1.0)
+            _, it, _, l, q = srv.result(rid)
+            lat.append(l)
+            queued.append(q)
+            sweeps += it
+            srv.release(rid)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.stop()
+        p_rate, p_lat = plain_queue(arr)
+        sweep.append({"rate_factor": factor, "offered_per_s": lam, "served_solves_per_s": len(reqs) / wall,
+                      "served_p50_s": float(np.percentile(lat, 50)), "served_p99_s": float(np.percentile(lat, 99)),
+                      "served_queue_p99_s": float(np.percentile(queued, 99)), "intervals": st["intervals"],
+                      "plain_solves_per_s": p_rate, "plain_p50_s": float(np.percentile(p_lat, 50)),
+                      "plain_p99_s": float(np.percentile(p_lat, 99))})
+    top = sweep[-1]
+    if dist.rank == 0:
+        line = {"metric": "served stencil solves/s", "value": top["served_solves_per_s"], "unit": "solves/s",
+                "n_gpus": dist.world, "steps": 1, "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": f"{len(reqs)} requests: half 2-D Jacobi n^2 (n log-uniform [64,4096]), half "
+                                       f"3-D heat m^3 (m log-uniform [32,256]); U[0,1) init; residual <= {tol} "
+                                       f"every {check} sweeps or {cap} sweeps; HBM budget 120 GB; Poisson arrivals",
+                           "plain_capacity_per_s": plain_capacity, "plain_sample": len(service)},
+                "sweep": sweep, "served_over_plain_at_top_rate": top["served_solves_per_s"] / top["plain_solves_per_s"]}
+        print(json.dumps(line), flush=True)
+
+
 def run_batch(args, dist: Dist):
     """Batched solves (BASELINE configs[3]): solves/s of the batched path, the
     one-grid-at-a-time GPU path on a size-stratified sample, and the error of
@@ -697,11 +799,14 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="stencil_suite", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="stencil_suite", choices=sorted(WORKLOADS) + ["serve"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-cap", type=int, default=0, help="sweep cap of the batch workloads")
     ap.add_argument("--batch-grids", type=int, default=0, help="number of grids of the batch workloads")
+    ap.add_argument("--serve-requests", type=int, default=400, help="requests of the serve workload (configs: 10000)")
+    ap.add_argument("--serve-plain-sample", type=int, default=40)
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[0.25, 0.5, 1.0, 2.0])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -713,6 +818,10 @@ def main():
 
     if args.workload.startswith("batch"):
         run_batch(args, dist)
+        dist.close()
+        return
+    if args.workload == "serve":
+        run_serve(args, dist)
         dist.close()
         return
 

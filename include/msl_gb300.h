@@ -230,6 +230,36 @@ int msl_batch_get_grid(void *batch, int index, float *host_out, long long *iters
 int msl_batch_info(void *batch, int *count, int *resident, long long *tiles, size_t *device_bytes);
 int msl_batch_destroy(void *batch);
 
+/* ---- stencil-solve server ------------------------------------------------------
+ * Continuous batching of solve requests: a worker thread admits requests in
+ * arrival order while their two iterates fit in hbm_budget (0 = no limit),
+ * advances all admitted requests together, check_every sweeps at a time (2-D
+ * and 3-D requests on two streams, overlapping), and retires each one when its
+ * FP64 residual max |last - previous| is <= tol or after max_iters sweeps
+ * (check_every must divide max_iters). A request's sweeps are those of the
+ * one-request path (msl_stencil2d_iterate / msl_stencil3d_iterate in chunks of
+ * check_every sweeps), so its result does not depend on what else is served.
+ * depth = fused sweeps per 2-D launch (0 = autotuned). No reference
+ * counterpart. */
+#define MSL_SERVE_JACOBI2D 0 /* plain Jacobi (MSL_ST2_JACOBI5) on rows x cols, FP32 */
+#define MSL_SERVE_HEAT3D 1   /* heat3D (MSL_ST3_HEAT7), Dirichlet 0, on depth x rows x cols, FP32 */
+int msl_server_start(size_t hbm_budget, double tol, long long max_iters, int check_every, int depth, void **server);
+/* Queue a request; `init` (FP32 host values) is copied, *request receives its id.
+ * A request larger than the whole budget fails with MSL_ERR_BUDGET. */
+int msl_server_submit(void *server, int kind, int depth, int rows, int cols, const float *init, long long *request);
+/* Block until the request finished (timeout_s < 0: no limit; MSL_ERR_TIMEOUT on expiry). */
+int msl_server_wait(void *server, long long request, double timeout_s);
+/* Result of a finished request: values (FP32, host), sweeps, last residual,
+ * latency (submit to completion) and queueing time (submit to admission). */
+int msl_server_result(void *server, long long request, float *out, long long *iters, double *residual,
+                      double *latency_s, double *queue_s);
+/* Forget a finished request (frees its host copy of the result). */
+int msl_server_release(void *server, long long request);
+int msl_server_stats(void *server, long long *completed, long long *active, long long *queued, size_t *device_bytes,
+                     long long *intervals);
+/* Serve what was submitted, then stop the worker and free the device state. */
+int msl_server_stop(void *server);
+
 /* ---- autotuner -------------------------------------------------------------
  * Times msl_stencil2d_iterate over `iters` sweeps of a rows x cols grid for
  * every temporal depth that fits (1, 2, 3, 4, 6, 8), on scratch grids it

@@ -76,6 +76,14 @@ def load() -> ctypes.CDLL:
         "msl_batch_get_grid": [vp, i, vp, ctypes.POINTER(ctypes.c_longlong), dp],
         "msl_batch_info": [vp, ip, ip, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(sz)],
         "msl_batch_destroy": [vp], "msl_batch_reset": [vp],
+        "msl_server_start": [sz, d, ctypes.c_longlong, i, i, ctypes.POINTER(vp)],
+        "msl_server_submit": [vp, i, i, i, i, vp, ctypes.POINTER(ctypes.c_longlong)],
+        "msl_server_wait": [vp, ctypes.c_longlong, d],
+        "msl_server_result": [vp, ctypes.c_longlong, vp, ctypes.POINTER(ctypes.c_longlong), dp, dp, dp],
+        "msl_server_release": [vp, ctypes.c_longlong],
+        "msl_server_stats": [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                             ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(sz), ctypes.POINTER(ctypes.c_longlong)],
+        "msl_server_stop": [vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -193,18 +201,82 @@ class Batch:
 
 
 def solve_plain(kind: int, grid: DeviceArray, other: DeviceArray, tol: float, max_iters: int, check_every: int):
-    """One grid at a time: msl_stencil2d_iterate in chunks of check_every sweeps
-    until the residual is <= tol. Returns (array holding the result, sweeps, residual)."""
+    """One grid at a time: msl_stencil2d_iterate (2-D arrays) or
+    msl_stencil3d_iterate (3-D arrays, neutral 0) in chunks of check_every
+    sweeps until the residual is <= tol. Returns (array holding the result,
+    sweeps, residual)."""
     a, b = grid, other
     it, res = 0, float("inf")
+    step = stencil3d_iterate if len(grid.shape) == 3 else stencil2d_iterate
     while it < max_iters:
-        last, res = stencil2d_iterate(kind, a, b, 1, 0.0, check_every)
+        last, res = step(kind, a, b, 1, 0.0, check_every)
         it += check_every
         if last is b:
             a, b = b, a
         if not res > tol:
             break
     return a, it, res
+
+
+class Server:
+    """Stencil-solve server (msl_server_*): continuous batching of 2-D Jacobi
+    and 3-D heat solves."""
+
+    def __init__(self, hbm_budget: int = 0, tol: float = 1e-4, max_iters: int = 5000, check_every: int = 100,
+                 depth: int = 0):
+        h = ctypes.c_void_p()
+        self.handle = None
+        check(load().msl_server_start(hbm_budget, tol, max_iters, check_every, depth, ctypes.byref(h)),
+              "msl_server_start")
+        self.handle = h
+        self.shapes = {}
+
+    def submit(self, init: np.ndarray) -> int:
+        """A 2-D array is a plain-Jacobi request, a 3-D array a heat3D request."""
+        a = np.ascontiguousarray(init, dtype=np.float32)
+        rid = ctypes.c_longlong()
+        if a.ndim == 2:
+            kind, dims = MSL_SERVE_JACOBI2D, (1, a.shape[0], a.shape[1])  # noqa: F821
+        else:
+            kind, dims = MSL_SERVE_HEAT3D, a.shape  # noqa: F821
+        check(load().msl_server_submit(self.handle, kind, dims[0], dims[1], dims[2], a.ctypes.data, ctypes.byref(rid)),
+              "msl_server_submit")
+        self.shapes[rid.value] = a.shape
+        return rid.value
+
+    def wait(self, rid: int, timeout: float = -1.0) -> None:
+        check(load().msl_server_wait(self.handle, rid, timeout), "msl_server_wait")
+
+    def result(self, rid: int):
+        """(values, sweeps, residual, latency_s, queue_s) of a finished request."""
+        out = np.empty(self.shapes[rid], np.float32)
+        it, res, lat, q = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(load().msl_server_result(self.handle, rid, out.ctypes.data, ctypes.byref(it), ctypes.byref(res),
+                                       ctypes.byref(lat), ctypes.byref(q)), "msl_server_result")
+        return out, it.value, res.value, lat.value, q.value
+
+    def release(self, rid: int) -> None:
+        check(load().msl_server_release(self.handle, rid), "msl_server_release")
+        self.shapes.pop(rid, None)
+
+    def stats(self):
+        c, a, q, i = (ctypes.c_longlong() for _ in range(4))
+        b = ctypes.c_size_t()
+        check(load().msl_server_stats(self.handle, ctypes.byref(c), ctypes.byref(a), ctypes.byref(q), ctypes.byref(b),
+                                      ctypes.byref(i)), "msl_server_stats")
+        return {"completed": c.value, "active": a.value, "queued": q.value, "device_bytes": b.value,
+                "intervals": i.value}
+
+    def stop(self) -> None:
+        if self.handle:
+            h, self.handle = self.handle, None
+            check(load().msl_server_stop(h), "msl_server_stop")
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass
 
 
 def device_info():

@@ -30,6 +30,7 @@ struct Batch {
     std::vector<void *> init;  // initial values of each grid (msl_batch_reset restores them)
     BatchGrid *dev = nullptr;
     int *d_lists = nullptr;  // resident list | work list
+    int *d_tile_grid = nullptr;  // work-list tile -> position of its grid in the work list
     int *d_active = nullptr;
     int *h_active = nullptr;  // pinned
     std::vector<int> resident, worklist;
@@ -52,6 +53,7 @@ void destroy(Batch *b) {
     if (b->pool) cudaFree(b->pool);
     if (b->dev) cudaFree(b->dev);
     if (b->d_lists) cudaFree(b->d_lists);
+    if (b->d_tile_grid) cudaFree(b->d_tile_grid);
     if (b->d_active) cudaFree(b->d_active);
     if (b->h_active) cudaFreeHost(b->h_active);
     if (b->side) cudaStreamDestroy(b->side);
@@ -111,7 +113,7 @@ int solve_t(Batch &b, double tol, long long max_iters, int check_every, int dept
         int per_sm = 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rk, kSt2Threads, smem);
         const long long grid = std::max(1LL, std::min<long long>(b.total_tiles, (long long)std::max(per_sm, 1) * c.sm_count));
-        // Rounds per graph: even (parity returns to 0) and a whole number of check chunks.
+        // Rounds per graph: a whole number of check chunks (and at least 8).
         const int chunk_rounds = check_every / depth;
         int rounds = chunk_rounds % 2 ? 2 * chunk_rounds : chunk_rounds;
         while (rounds < 8) rounds *= 2;
@@ -120,9 +122,8 @@ int solve_t(Batch &b, double tol, long long max_iters, int check_every, int dept
         MSL_TRY_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "msl_batch_solve: capture");
         for (int j = 0; j < rounds; j++) {
             const int check = ((j + 1) % chunk_rounds) == 0;
-            rk<<<(unsigned)grid, kSt2Threads, smem, st>>>(b.dev, wl, nlist, b.total_tiles, j & 1, depth, check);
-            batch_finalize_kernel<<<1, 256, 0, st>>>(b.dev, wl, nlist, depth, (j + 1) & 1, check, tol, max_iters,
-                                                      b.d_active);
+            rk<<<(unsigned)grid, kSt2Threads, smem, st>>>(b.dev, wl, b.d_tile_grid, b.total_tiles, depth, check);
+            batch_finalize_kernel<<<1, 256, 0, st>>>(b.dev, wl, nlist, depth, check, tol, max_iters, b.d_active);
         }
         cudaError_t ce = cudaStreamEndCapture(st, &graph);
         if (ce != cudaSuccess) return rt::cuda_fail(ce, "msl_batch_solve: capture");
@@ -224,6 +225,16 @@ int msl_batch_create(int storage, int count, const int *rows, const int *cols, s
     std::vector<int> lists(b->resident);
     lists.insert(lists.end(), b->worklist.begin(), b->worklist.end());
     e = cudaMemcpy(b->d_lists, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && b->total_tiles) {
+        std::vector<int> tg((size_t)b->total_tiles);
+        for (size_t w = 0; w < b->worklist.size(); w++) {
+            const BatchGrid &gd = b->host[b->worklist[w]];
+            const long long nt = (long long)((gd.cols + kSt2BX - 1) / kSt2BX) * ((gd.rows + kSt2BY - 1) / kSt2BY);
+            for (long long t = 0; t < nt; t++) tg[(size_t)(gd.first_tile + t)] = (int)w;
+        }
+        e = cudaMalloc(&b->d_tile_grid, tg.size() * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemcpy(b->d_tile_grid, tg.data(), tg.size() * sizeof(int), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMemset(b->pool, 0, b->pool_bytes);
     if (e != cudaSuccess) {
         destroy(b);

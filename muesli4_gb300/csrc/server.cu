@@ -1,0 +1,482 @@
+// Stencil-solve server of libmsl_gb300.so (msl_server_*): continuous batching
+// of plain-Jacobi (2-D) and heat3D (3-D) solve requests.
+//
+// A worker thread owns the device side. Every iteration of its loop it
+// (1) admits queued requests in arrival order while their iterates fit in the
+//     HBM budget (stream-ordered allocation from the device's memory pool,
+//     host-to-device copy of the initial values),
+// (2) advances every active request by one check interval of `check_every`
+//     sweeps -- all 2-D requests in one tile work-list (batch_round_kernel,
+//     `depth` fused sweeps per launch) and all 3-D requests in another
+//     (serve3d_round_kernel), on two streams so their work overlaps -- and
+//     takes each request's FP64 residual at the end of the interval,
+// (3) retires requests whose residual is <= tol or that reached max_iters:
+//     copies the result to host memory, frees its iterates, stamps its
+//     completion time.
+// Requests that arrive while others run join at the next interval, as slots
+// and memory free up. Each request's sweeps are exactly those of
+// msl_stencil2d_iterate / msl_stencil3d_iterate run on it alone in chunks of
+// check_every sweeps, so its result does not depend on what else is served.
+//
+// No reference counterpart: the reference solves one container at a time.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../include/detail/msl_serve.cuh"
+#include "msl_internal.h"
+
+using namespace msl;
+using namespace msl::gpu;
+using msl::rt::ctx;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+constexpr int kMaxActive = 4096;  // active requests of each kind
+
+enum ReqState { kQueued = 0, kRunning = 1, kDone = 2, kFailed = 3 };
+
+struct Request {
+    long long id = 0;
+    int kind = 0;  // MSL_SERVE_JACOBI2D / MSL_SERVE_HEAT3D
+    int depth = 1, rows = 0, cols = 0;
+    std::vector<float> init, out;
+    Clock::time_point t_submit, t_admit, t_done;
+    size_t bytes = 0;  // both iterates
+    void *buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    long long iters = 0;
+    double residual = 0.0;
+    int state = kQueued;     // read and written under the server lock
+    bool finished = false;   // set by the worker when the request converged or ran out of sweeps
+    size_t cells() const { return (size_t)depth * rows * cols; }
+};
+
+struct Server {
+    size_t budget = 0, used = 0;
+    double tol = 1e-4;
+    long long max_iters = 5000;
+    int check_every = 100, depth2d = 1;
+    int device = 0, sm_count = 152;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    bool stop = false;
+    std::string error;
+    long long next_id = 1, completed = 0, intervals = 0;
+    std::deque<Request *> queue;
+    std::vector<Request *> active;
+    std::map<long long, std::unique_ptr<Request>> all;
+    cudaStream_t s2 = nullptr, s3 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    BatchGrid *d2 = nullptr;
+    ServeCube *d3 = nullptr;
+    int *dlist = nullptr;  // 0..kMaxActive-1
+    int *d_active = nullptr;
+    int *d_map2 = nullptr, *d_map3 = nullptr;  // tile -> request, block -> request (grown as needed)
+    size_t cap_map2 = 0, cap_map3 = 0;
+    std::vector<int> map2, map3;
+    std::vector<BatchGrid> h2;
+    std::vector<ServeCube> h3;
+};
+
+size_t iterate_bytes(const Request &r) { return 2 * ((r.cells() * sizeof(float) + 255) / 256 * 256); }
+
+void fail_all(Server &s, const std::string &why) {
+    std::lock_guard<std::mutex> g(s.mu);
+    s.error = why;
+    for (auto &kv : s.all)
+        if (kv.second->state == kQueued || kv.second->state == kRunning) kv.second->state = kFailed;
+    s.queue.clear();
+    s.active.clear();
+    s.cv_done.notify_all();
+}
+
+#define SERVE_TRY(call)                      \
+    do {                                     \
+        cudaError_t _e = (call);             \
+        if (_e != cudaSuccess) return _e;    \
+    } while (0)
+
+// Copy an item -> request map to the device, growing its buffer when needed.
+// The host vector stays alive until the interval's synchronisation.
+cudaError_t upload_map(const std::vector<int> &m, int **d, size_t *cap, cudaStream_t st) {
+    if (m.size() > *cap) {
+        if (*d) SERVE_TRY(cudaFreeAsync(*d, st));
+        const size_t n = std::max(m.size(), 2 * *cap);
+        SERVE_TRY(cudaMallocAsync((void **)d, n * sizeof(int), st));
+        *cap = n;
+    }
+    return cudaMemcpyAsync(*d, m.data(), m.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+}
+
+// One check interval (check_every sweeps) for every active request.
+cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
+    s.h2.clear();
+    s.h3.clear();
+    s.map2.clear();
+    s.map3.clear();
+    std::vector<Request *> r2, r3;
+    long long tiles = 0, blocks = 0;
+    for (Request *r : act) {
+        if (r->kind == MSL_SERVE_JACOBI2D) {
+            BatchGrid g{};
+            g.buf[0] = r->buf[0];
+            g.buf[1] = r->buf[1];
+            g.rows = r->rows;
+            g.cols = r->cols;
+            g.cur = r->cur;
+            g.iters = r->iters;
+            g.first_tile = tiles;
+            const long long nt = (long long)((r->cols + kSt2BX - 1) / kSt2BX) * ((r->rows + kSt2BY - 1) / kSt2BY);
+            tiles += nt;
+            s.map2.insert(s.map2.end(), (size_t)nt, (int)s.h2.size());
+            s.h2.push_back(g);
+            r2.push_back(r);
+        } else {
+            ServeCube c{};
+            c.buf[0] = r->buf[0];
+            c.buf[1] = r->buf[1];
+            c.depth = r->depth;
+            c.rows = r->rows;
+            c.cols = r->cols;
+            c.cur = r->cur;
+            c.iters = r->iters;
+            c.first_block = blocks;
+            const long long nb = (long long)((r->cols + kT3BX - 1) / kT3BX) * ((r->rows + kT3BY - 1) / kT3BY) *
+                                 ((r->depth + kT3BZ - 1) / kT3BZ);
+            blocks += nb;
+            s.map3.insert(s.map3.end(), (size_t)nb, (int)s.h3.size());
+            s.h3.push_back(c);
+            r3.push_back(r);
+        }
+    }
+    const int n2 = (int)s.h2.size(), n3 = (int)s.h3.size();
+    SERVE_TRY(cudaEventRecord(s.ev_fork, s.s2));
+    SERVE_TRY(cudaStreamWaitEvent(s.s3, s.ev_fork, 0));
+    if (n2) {
+        SERVE_TRY(cudaMemcpyAsync(s.d2, s.h2.data(), n2 * sizeof(BatchGrid), cudaMemcpyHostToDevice, s.s2));
+        SERVE_TRY(upload_map(s.map2, &s.d_map2, &s.cap_map2, s.s2));
+        const int depth = s.depth2d;
+        const size_t smem = stencil2d_tb_smem<float>(1, depth);
+        auto rk = batch_round_kernel<float>;
+        if (smem > 48 * 1024) SERVE_TRY(cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rk, kSt2Threads, smem);
+        const long long grid = std::max(1LL, std::min<long long>(tiles, (long long)std::max(per_sm, 1) * s.sm_count));
+        const int launches = s.check_every / depth;
+        for (int j = 0; j < launches; j++) {
+            const int check = j == launches - 1;
+            rk<<<(unsigned)grid, kSt2Threads, smem, s.s2>>>(s.d2, s.dlist, s.d_map2, tiles, depth, check);
+            batch_finalize_kernel<<<1, 256, 0, s.s2>>>(s.d2, s.dlist, n2, depth, check, s.tol, s.max_iters,
+                                                        s.d_active);
+        }
+        SERVE_TRY(cudaGetLastError());
+        rt::count_launch(2 * launches);
+        SERVE_TRY(cudaMemcpyAsync(s.h2.data(), s.d2, n2 * sizeof(BatchGrid), cudaMemcpyDeviceToHost, s.s2));
+    }
+    if (n3) {
+        SERVE_TRY(cudaMemcpyAsync(s.d3, s.h3.data(), n3 * sizeof(ServeCube), cudaMemcpyHostToDevice, s.s3));
+        SERVE_TRY(upload_map(s.map3, &s.d_map3, &s.cap_map3, s.s3));
+        const size_t smem = serve3d_smem();
+        SERVE_TRY(cudaFuncSetAttribute(serve3d_round_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, serve3d_round_kernel, kT3Threads, smem);
+        const long long grid = std::max(1LL, std::min<long long>(blocks, (long long)std::max(per_sm, 1) * s.sm_count));
+        for (int j = 0; j < s.check_every; j++) {
+            const int check = j == s.check_every - 1;
+            serve3d_round_kernel<<<(unsigned)grid, kT3Threads, smem, s.s3>>>(s.d3, s.dlist, s.d_map3, blocks, check);
+            serve3d_finalize_kernel<<<1, 256, 0, s.s3>>>(s.d3, s.dlist, n3, check, s.tol, s.max_iters);
+        }
+        SERVE_TRY(cudaGetLastError());
+        rt::count_launch(2 * s.check_every);
+        SERVE_TRY(cudaMemcpyAsync(s.h3.data(), s.d3, n3 * sizeof(ServeCube), cudaMemcpyDeviceToHost, s.s3));
+    }
+    SERVE_TRY(cudaEventRecord(s.ev_join, s.s3));
+    SERVE_TRY(cudaStreamWaitEvent(s.s2, s.ev_join, 0));
+    SERVE_TRY(cudaStreamSynchronize(s.s2));
+    for (int i = 0; i < n2; i++) {
+        Request *r = r2[i];
+        r->cur = s.h2[i].cur;
+        r->iters = s.h2[i].iters;
+        r->residual = s.h2[i].residual;
+        r->finished = s.h2[i].done != 0;
+    }
+    for (int i = 0; i < n3; i++) {
+        Request *r = r3[i];
+        r->cur = s.h3[i].cur;
+        r->iters = s.h3[i].iters;
+        r->residual = s.h3[i].residual;
+        r->finished = s.h3[i].done != 0;
+    }
+    return cudaSuccess;
+}
+
+void worker_loop(Server *sp) {
+    Server &s = *sp;
+    cudaSetDevice(s.device);
+    for (;;) {
+        std::vector<Request *> act;
+        {
+            std::unique_lock<std::mutex> g(s.mu);
+            // admit in arrival order while memory and slots allow
+            int n2 = 0, n3 = 0;
+            for (Request *r : s.active) (r->kind == MSL_SERVE_JACOBI2D ? n2 : n3)++;
+            while (!s.queue.empty()) {
+                Request *r = s.queue.front();
+                int &n = r->kind == MSL_SERVE_JACOBI2D ? n2 : n3;
+                if (n >= kMaxActive || (s.budget && s.used + r->bytes > s.budget)) break;
+                s.queue.pop_front();
+                s.used += r->bytes;
+                n++;
+                r->state = kRunning;
+                r->t_admit = Clock::now();
+                s.active.push_back(r);
+                // allocation and upload happen below, outside the lock
+                r->buf[0] = nullptr;
+            }
+            if (s.active.empty()) {
+                if (s.stop) return;
+                s.cv_work.wait(g, [&] { return s.stop || !s.queue.empty(); });
+                continue;
+            }
+            act = s.active;
+        }
+        bool ok = true;
+        std::string why;
+        for (Request *r : act) {
+            if (r->buf[0]) continue;
+            const size_t half = r->bytes / 2;
+            void *p = nullptr;
+            cudaError_t e = cudaMallocAsync(&p, r->bytes, s.s2);
+            if (e == cudaSuccess) {
+                r->buf[0] = p;
+                r->buf[1] = (char *)p + half;
+                r->cur = 0;
+                r->iters = 0;
+                e = cudaMemcpyAsync(r->buf[0], r->init.data(), r->cells() * sizeof(float), cudaMemcpyHostToDevice, s.s2);
+            }
+            if (e != cudaSuccess) {
+                ok = false;
+                why = std::string("admission: ") + cudaGetErrorString(e);
+                break;
+            }
+        }
+        if (ok) {
+            cudaError_t e = run_interval(s, act);
+            if (e != cudaSuccess) {
+                ok = false;
+                why = std::string("interval: ") + cudaGetErrorString(e);
+            }
+        }
+        if (!ok) {
+            fail_all(s, why);
+            return;
+        }
+        s.intervals++;
+        // retire finished requests
+        std::vector<Request *> done;
+        for (Request *r : act)
+            if (r->finished) done.push_back(r);
+        for (Request *r : done) {
+            r->out.resize(r->cells());
+            cudaError_t e = cudaMemcpyAsync(r->out.data(), r->buf[r->cur], r->cells() * sizeof(float),
+                                            cudaMemcpyDeviceToHost, s.s2);
+            if (e == cudaSuccess) e = cudaFreeAsync(r->buf[0], s.s2);
+            if (e != cudaSuccess) {
+                fail_all(s, std::string("retire: ") + cudaGetErrorString(e));
+                return;
+            }
+        }
+        if (!done.empty()) {
+            cudaStreamSynchronize(s.s2);
+            const auto now = Clock::now();
+            std::lock_guard<std::mutex> g(s.mu);
+            for (Request *r : done) {
+                r->state = kDone;
+                r->t_done = now;
+                r->buf[0] = r->buf[1] = nullptr;
+                r->init.clear();
+                r->init.shrink_to_fit();
+                s.used -= r->bytes;
+                s.completed++;
+                s.active.erase(std::find(s.active.begin(), s.active.end(), r));
+            }
+            s.cv_done.notify_all();
+        }
+    }
+}
+
+Server *as_server(void *p) { return (Server *)p; }
+
+}  // namespace
+
+extern "C" {
+
+int msl_server_start(size_t hbm_budget, double tol, long long max_iters, int check_every, int depth, void **server) {
+    auto &c = ctx();
+    if (int e = rt::require_init()) return e;
+    if (!server || check_every < 1 || max_iters < 1 || max_iters % check_every)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_start: check_every must be >= 1 and divide max_iters");
+    if (depth <= 0) depth = rt::tuned_depth(MSL_F32, MSL_ST2_JACOBI5, 1024, 1024, 1);
+    while (depth > 1 && check_every % depth) depth--;
+    auto *s = new Server;
+    s->budget = hbm_budget;
+    s->tol = tol;
+    s->max_iters = max_iters;
+    s->check_every = check_every;
+    s->depth2d = std::min(depth, 8);
+    s->device = c.device;
+    s->sm_count = c.sm_count;
+    cudaError_t e = cudaStreamCreateWithFlags(&s->s2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s3, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d2, kMaxActive * sizeof(BatchGrid));
+    if (e == cudaSuccess) e = cudaMalloc(&s->d3, kMaxActive * sizeof(ServeCube));
+    if (e == cudaSuccess) e = cudaMalloc(&s->dlist, kMaxActive * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_active, sizeof(int));
+    if (e == cudaSuccess) {
+        std::vector<int> iota(kMaxActive);
+        for (int i = 0; i < kMaxActive; i++) iota[i] = i;
+        e = cudaMemcpy(s->dlist, iota.data(), kMaxActive * sizeof(int), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+        // keep freed iterates in the pool for the next admissions (up to the budget)
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, c.device) == cudaSuccess) {
+            cuuint64_t keep = hbm_budget ? hbm_budget : ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
+    if (e != cudaSuccess) {
+        delete s;
+        return rt::cuda_fail(e, "msl_server_start");
+    }
+    s->worker = std::thread(worker_loop, s);
+    *server = s;
+    return MSL_OK;
+}
+
+int msl_server_submit(void *server, int kind, int depth, int rows, int cols, const float *init, long long *request) {
+    Server *s = as_server(server);
+    if (!s || !init || !request) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_submit: NULL argument");
+    if (kind != MSL_SERVE_JACOBI2D && kind != MSL_SERVE_HEAT3D)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_submit: unknown kind %d", kind);
+    if (kind == MSL_SERVE_JACOBI2D) depth = 1;
+    if (depth < 1 || rows < 1 || cols < 1 || (long long)depth * rows * cols > (1LL << 31) - 1)
+        return rt::fail(MSL_ERR_SIZE_MISMATCH, "msl_server_submit: bad shape %d x %d x %d", depth, rows, cols);
+    auto r = std::make_unique<Request>();
+    r->kind = kind;
+    r->depth = depth;
+    r->rows = rows;
+    r->cols = cols;
+    r->init.assign(init, init + r->cells());
+    r->bytes = iterate_bytes(*r);
+    if (s->budget && r->bytes > s->budget)
+        return rt::fail(MSL_ERR_BUDGET, "msl_server_submit: request needs %zu bytes, budget %zu", r->bytes, s->budget);
+    std::lock_guard<std::mutex> g(s->mu);
+    if (!s->error.empty()) return rt::fail(MSL_ERR_CUDA, "msl_server_submit: server failed: %s", s->error.c_str());
+    if (s->stop) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_submit: server is stopping");
+    r->id = s->next_id++;
+    r->t_submit = Clock::now();
+    *request = r->id;
+    s->queue.push_back(r.get());
+    s->all[r->id] = std::move(r);
+    s->cv_work.notify_one();
+    return MSL_OK;
+}
+
+int msl_server_wait(void *server, long long request, double timeout_s) {
+    Server *s = as_server(server);
+    if (!s) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_wait: NULL server");
+    std::unique_lock<std::mutex> g(s->mu);
+    auto it = s->all.find(request);
+    if (it == s->all.end()) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_wait: unknown request %lld", request);
+    Request *r = it->second.get();
+    auto pred = [&] { return r->state == kDone || r->state == kFailed; };
+    if (timeout_s < 0) s->cv_done.wait(g, pred);
+    else if (!s->cv_done.wait_for(g, std::chrono::duration<double>(timeout_s), pred))
+        return rt::fail(MSL_ERR_TIMEOUT, "msl_server_wait: request %lld not finished", request);
+    if (r->state == kFailed) return rt::fail(MSL_ERR_CUDA, "msl_server_wait: %s", s->error.c_str());
+    return MSL_OK;
+}
+
+int msl_server_result(void *server, long long request, float *out, long long *iters, double *residual,
+                      double *latency_s, double *queue_s) {
+    Server *s = as_server(server);
+    if (!s) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_result: NULL server");
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->all.find(request);
+    if (it == s->all.end()) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_result: unknown request %lld", request);
+    Request *r = it->second.get();
+    if (r->state != kDone) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_result: request %lld not done", request);
+    if (out) std::memcpy(out, r->out.data(), r->out.size() * sizeof(float));
+    if (iters) *iters = r->iters;
+    if (residual) *residual = r->residual;
+    if (latency_s) *latency_s = std::chrono::duration<double>(r->t_done - r->t_submit).count();
+    if (queue_s) *queue_s = std::chrono::duration<double>(r->t_admit - r->t_submit).count();
+    return MSL_OK;
+}
+
+int msl_server_release(void *server, long long request) {
+    Server *s = as_server(server);
+    if (!s) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_release: NULL server");
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->all.find(request);
+    if (it == s->all.end() || it->second->state != kDone)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_release: request %lld is not a finished request", request);
+    s->all.erase(it);
+    return MSL_OK;
+}
+
+int msl_server_stats(void *server, long long *completed, long long *active, long long *queued, size_t *device_bytes,
+                     long long *intervals) {
+    Server *s = as_server(server);
+    if (!s) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_stats: NULL server");
+    std::lock_guard<std::mutex> g(s->mu);
+    if (completed) *completed = s->completed;
+    if (active) *active = (long long)s->active.size();
+    if (queued) *queued = (long long)s->queue.size();
+    if (device_bytes) *device_bytes = s->used;
+    if (intervals) *intervals = s->intervals;
+    return MSL_OK;
+}
+
+int msl_server_stop(void *server) {
+    Server *s = as_server(server);
+    if (!s) return MSL_OK;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        s->stop = true;
+        s->cv_work.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    for (auto &kv : s->all)
+        if (kv.second->buf[0]) cudaFreeAsync(kv.second->buf[0], s->s2);
+    cudaStreamSynchronize(s->s2);
+    cudaFree(s->d2);
+    cudaFree(s->d3);
+    cudaFree(s->dlist);
+    cudaFree(s->d_active);
+    if (s->d_map2) cudaFree(s->d_map2);
+    if (s->d_map3) cudaFree(s->d_map3);
+    cudaEventDestroy(s->ev_fork);
+    cudaEventDestroy(s->ev_join);
+    cudaStreamDestroy(s->s2);
+    cudaStreamDestroy(s->s3);
+    std::string err = s->error;
+    delete s;
+    if (!err.empty()) return rt::fail(MSL_ERR_CUDA, "msl_server_stop: the server had failed: %s", err.c_str());
+    return MSL_OK;
+}
+
+}  // extern "C"

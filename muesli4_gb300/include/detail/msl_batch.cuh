@@ -123,12 +123,13 @@ __global__ void __launch_bounds__(kBatchResidentThreads)
 }
 
 // One round of the work-list grids: every tile of every unfinished grid does
-// `depth` sweeps from buf[parity] to buf[parity ^ 1]. Plain coalesced loads
+// `depth` sweeps from buf[cur] to buf[cur ^ 1] (each grid's own direction, so
+// grids that joined at different times can share a round). Plain coalesced loads
 // stage the windows (grids differ in pointer and shape). `check` marks the
 // round whose last sweep ends a residual-check chunk.
 template <typename S>
 __global__ void __launch_bounds__(kSt2Threads)
-    batch_round_kernel(BatchGrid *grids, const int *list, int nlist, long long total_tiles, int parity, int depth,
+    batch_round_kernel(BatchGrid *grids, const int *list, const int *tile_grid, long long total_tiles, int depth,
                        int check) {
     using T = typename Compute<S>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -141,17 +142,14 @@ __global__ void __launch_bounds__(kSt2Threads)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     JacobiFn fn;
     for (long long item = blockIdx.x; item < total_tiles; item += gridDim.x) {
-        // locate the grid of this tile (grids are few: linear scan of the prefix)
-        int gi = 0;
-        while (gi + 1 < nlist && grids[list[gi + 1]].first_tile <= item) gi++;
-        BatchGrid &g = grids[list[gi]];
+        BatchGrid &g = grids[list[tile_grid[item]]];  // tile_grid: work-list position of the tile's grid
         if (g.done) continue;  // uniform for the CTA
         const int rows = g.rows, cols = g.cols;
         const int tiles_x = (cols + kSt2BX - 1) / kSt2BX;
         const long long t = item - g.first_tile;
         const int x0 = (int)(t % tiles_x) * kSt2BX, y0 = (int)(t / tiles_x) * kSt2BY;
-        const S *in = (const S *)g.buf[parity];
-        S *out = (S *)g.buf[parity ^ 1];
+        const S *in = (const S *)g.buf[g.cur];
+        S *out = (S *)g.buf[g.cur ^ 1];
         const int wx0 = x0 - hx, wy0 = y0 - depth * r;
         __syncthreads();  // previous item's readers are done with the buffers
         for (int i = threadIdx.x; i < pitch * th; i += blockDim.x) {
@@ -176,14 +174,22 @@ __global__ void __launch_bounds__(kSt2Threads)
             const int ext = (depth - s) * r;
             const int W = kSt2BX + 2 * ext, H = kSt2BY + 2 * ext;
             const int gx0 = x0 - ext, gy0 = y0 - ext;
-            m.check_ = true;
-            for (int row = warp; row < H; row += nwarps) {
-                const int gy = gy0 + row;
-                if ((unsigned)gy >= (unsigned)rows) continue;
-                for (int col = lane; col < W; col += 32) {
-                    const int gx = gx0 + col;
-                    if ((unsigned)gx < (unsigned)cols) dst[(gy - wy0) * pitch + (gx - wx0)] = narrow<S>(fn(m, gx, gy));
+            auto sweep = [&](const NPLMatrix<T, S> &v) {
+                for (int row = warp; row < H; row += nwarps) {
+                    const int gy = gy0 + row;
+                    if ((unsigned)gy >= (unsigned)rows) continue;
+                    for (int col = lane; col < W; col += 32) {
+                        const int gx = gx0 + col;
+                        if ((unsigned)gx < (unsigned)cols) dst[(gy - wy0) * pitch + (gx - wx0)] = narrow<S>(fn(v, gx, gy));
+                    }
                 }
+            };
+            if (gx0 - r >= 0 && gy0 - r >= 0 && gx0 + W + r <= cols && gy0 + H + r <= rows) {
+                m.check_ = false;
+                sweep(m);
+            } else {
+                m.check_ = true;
+                sweep(m);
             }
             __syncthreads();
             m.tile_ = dst;
@@ -192,8 +198,13 @@ __global__ void __launch_bounds__(kSt2Threads)
         const int x = x0 + (warp % (kSt2BX / 32)) * 32 + lane;
         const int ys = y0 + (warp / (kSt2BX / 32)) * kSt2RPT;
         double dmax = 0.0;
-        m.check_ = true;
-        stencil2d_strip<S, false>(fn, m, x, ys, rows, cols, out, check != 0, dmax);
+        if (x0 - r >= 0 && y0 - r >= 0 && x0 + kSt2BX + r <= cols && y0 + kSt2BY + r <= rows) {
+            m.check_ = false;
+            stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, check != 0, dmax);
+        } else {
+            m.check_ = true;
+            stencil2d_strip<S, false>(fn, m, x, ys, rows, cols, out, check != 0, dmax);
+        }
         if (check) {
             dmax = block_max(dmax);
             if (threadIdx.x == 0) atomic_max_nonneg(&g.resid_bits, dmax);
@@ -204,7 +215,7 @@ __global__ void __launch_bounds__(kSt2Threads)
 // After a round: advance the sweep counts and, on a check round, take the
 // residuals and retire converged grids (and grids out of sweeps). Counts the
 // grids still running into *active.
-__global__ void batch_finalize_kernel(BatchGrid *grids, const int *list, int nlist, int depth, int parity_after,
+static __global__ void batch_finalize_kernel(BatchGrid *grids, const int *list, int nlist, int depth,
                                       int check, double tol, long long max_iters, int *active) {
     __shared__ int s_active;
     if (threadIdx.x == 0) s_active = 0;
@@ -213,7 +224,7 @@ __global__ void batch_finalize_kernel(BatchGrid *grids, const int *list, int nli
         BatchGrid &g = grids[list[i]];
         if (g.done) continue;
         g.iters += depth;
-        g.cur = parity_after;
+        g.cur ^= 1;
         if (check) {
             double r = __longlong_as_double((long long)g.resid_bits);
             g.residual = r;
