@@ -175,6 +175,48 @@ int msl_fold_absdiff_max(int dtype, const void *a, const void *b, size_t n, doub
  * No counterpart in the reference (its fold allocates per call, src/ds.cpp:772). */
 int msl_fold_noalloc(int dtype, int op, const void *in, size_t n, void *result_device, void *stream);
 
+/* ---- row / column skeletons of a rows x cols row-major matrix (DM) -------- */
+/* out[r] = fold of row r with op (MSL_FOLD_*), for every row. The fold order is
+ * the reference's row-fold kernel's: L lanes per row (L = threads_per_block when
+ * cols >= threads_per_block, else the next power of two >= (cols + 1) / 2);
+ * lane t folds row[t], row[t+L], ... left to right, then lane values combine
+ * pairwise v[t] = f(v[t], v[t+h]) for h = L/2 ... 1. threads_per_block is the
+ * reference's setThreadsPerBlock value: a power of two in [1, 1024].
+ * dtype MSL_F32, MSL_F64 or MSL_I32. Replaces DM::reduceRows
+ * (src/dm.cpp:1596-1707, kernel src/fold_kernels.cu:215-294). */
+int msl_fold_rows(int dtype, int op, const void *in, long long rows, long long cols, int threads_per_block,
+                  void *out);
+/* out[c] = fold of column c top to bottom (element-seeded, sequential):
+ * the column counterpart of msl_fold_rows. */
+int msl_fold_cols(int dtype, int op, const void *in, long long rows, long long cols, void *out);
+/* out[r][c] = op(m[r][c], v[r]) with a MSL_ZIP_* op: a matrix zipped with a
+ * per-row vector (the DM x DA broadcast of DM::zipIndexInPlaceA,
+ * src/dm.cpp:1790-1812). out may be m. */
+int msl_zip_rows(int dtype, int op, const void *m, const void *v, void *out, long long rows, long long cols);
+/* out row k = in row (k - a) mod rows. |a| > rows is MSL_ERR_NOT_IMPLEMENTED,
+ * as the reference's RotateRowManyNotImplementedException; out != in.
+ * Replaces DM::rotateRows (src/dm.cpp:1345-1475). Any dtype (a raw copy). */
+int msl_rotate_rows(int dtype, const void *in, void *out, long long rows, long long cols, long long a);
+/* out[r][j] = in[r][(j + a) mod cols]; out != in. Replaces DM::rotateCols
+ * (src/dm.cpp:1483-1533). */
+int msl_rotate_cols(int dtype, const void *in, void *out, long long rows, long long cols, long long a);
+/* dm[r][col] = da[r] for every row; col outside [0, cols) is
+ * MSL_ERR_INVALID_ARGUMENT. Replaces DM::setColumn (src/dm.cpp:1856-1879). */
+int msl_set_column(int dtype, void *dm, const void *da, long long rows, long long cols, long long col);
+
+/* ---- grid results I/O --------------------------------------------------------- */
+/* Append a device grid to a text file in the `;`-separated format of the
+ * reference's examples: depth 1 writes one line per row (examples/
+ * heatdiffusion.cpp:99-114); depth > 1 writes one line per (x, y) with z
+ * innermost (examples/heatdiffusion.cpp:156-170). Values are formatted as
+ * std::ostream writes them by default (%g, 6 significant digits; integers in
+ * decimal); bfloat16 values as the float they hold. */
+int msl_grid_dump_text(const char *path, int dtype, const void *grid, int depth, int rows, int cols);
+/* Read such a file back into a device grid (exactly depth*rows*cols values,
+ * else MSL_ERR_SIZE_MISMATCH). The text holds 6 significant digits: a dump
+ * and load round trip is exact for integers and for values with at most 6. */
+int msl_grid_load_text(const char *path, int dtype, void *grid, int depth, int rows, int cols);
+
 /* ---- stencils ------------------------------------------------------------- */
 /* Stage stencil windows with TMA tensor copies when the grid allows it (1,
  * the default) or always with plain coalesced loads (0). Results are
@@ -220,14 +262,26 @@ int msl_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int 
 int msl_batch_create(int storage, int count, const int *rows, const int *cols, size_t hbm_budget, void **batch);
 /* Set grid `index` from FP32 host values (rounded to bfloat16 for BF16 storage). */
 int msl_batch_set_grid(void *batch, int index, const float *host_grid);
-/* Restore every grid to the values last given by msl_batch_set_grid (device copy). */
+/* Restore every grid to the values last given by msl_batch_set_grid (device
+ * copy) and set its sweep count to 0. */
 int msl_batch_reset(void *batch);
-/* Iterate every grid; check_every must divide max_iters; depth 0 = autotuned. */
+/* Iterate every grid until its FP64 residual (checked every check_every
+ * sweeps) is <= tol or it has done max_iters sweeps in total. A grid continues
+ * from its own sweep count (0 after create, set_grid or reset), which must be
+ * a multiple of check_every; check_every must divide max_iters; depth 0 =
+ * autotuned. */
 int msl_batch_solve(void *batch, double tol, long long max_iters, int check_every, int depth);
 /* Latest iterate of grid `index` as FP32, with its sweep count and last residual. */
 int msl_batch_get_grid(void *batch, int index, float *host_out, long long *iters, double *residual);
 /* Grid count, grids solved CTA-resident, work-list tiles, device bytes (iterates and initial values). */
 int msl_batch_info(void *batch, int *count, int *resident, long long *tiles, size_t *device_bytes);
+/* Write the batch to a file: every grid's shape, sweep count, residual and
+ * done flag, its latest iterate and its initial values. */
+int msl_batch_checkpoint(void *batch, const char *path);
+/* Create a batch from a checkpoint file (under hbm_budget, 0 = no limit).
+ * msl_batch_solve then resumes every grid from its sweep count: with the same
+ * tol and check_every the results equal those of one uninterrupted solve. */
+int msl_batch_restore(const char *path, size_t hbm_budget, void **batch);
 int msl_batch_destroy(void *batch);
 
 /* ---- stencil-solve server ------------------------------------------------------

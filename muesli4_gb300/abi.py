@@ -56,6 +56,7 @@ def load() -> ctypes.CDLL:
     L = ctypes.CDLL(LIB_PATH)
     i, sz, d, vp = ctypes.c_int, ctypes.c_size_t, ctypes.c_double, ctypes.c_void_p
     dp, ip, llp = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)
+    ll = ctypes.c_longlong
     sig = {
         "msl_init": [i], "msl_terminate": [], "msl_sync": [], "msl_get_stream": [ctypes.POINTER(vp)],
         "msl_set_stream": [vp], "msl_device_info": [ip, ctypes.POINTER(sz), ctypes.POINTER(sz)],
@@ -71,11 +72,16 @@ def load() -> ctypes.CDLL:
         "msl_set_temporal_depth": [i], "msl_autotune_stencil2d": [i, i, i, i, i, i, ip, dp],
         "msl_autotune_save": [ctypes.c_char_p], "msl_autotune_load": [ctypes.c_char_p],
         "msl_fold_noalloc": [i, i, vp, sz, vp, vp],
+        "msl_fold_rows": [i, i, vp, ll, ll, i, vp], "msl_fold_cols": [i, i, vp, ll, ll, vp],
+        "msl_zip_rows": [i, i, vp, vp, vp, ll, ll], "msl_rotate_rows": [i, vp, vp, ll, ll, ll],
+        "msl_rotate_cols": [i, vp, vp, ll, ll, ll], "msl_set_column": [i, vp, vp, ll, ll, ll],
         "msl_batch_create": [i, i, ip, ip, sz, ctypes.POINTER(vp)], "msl_batch_set_grid": [vp, i, vp],
         "msl_batch_solve": [vp, d, ctypes.c_longlong, i, i],
         "msl_batch_get_grid": [vp, i, vp, ctypes.POINTER(ctypes.c_longlong), dp],
         "msl_batch_info": [vp, ip, ip, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(sz)],
         "msl_batch_destroy": [vp], "msl_batch_reset": [vp],
+        "msl_grid_dump_text": [ctypes.c_char_p, i, vp, i, i, i], "msl_grid_load_text": [ctypes.c_char_p, i, vp, i, i, i],
+        "msl_batch_checkpoint": [vp, ctypes.c_char_p], "msl_batch_restore": [ctypes.c_char_p, sz, ctypes.POINTER(vp)],
         "msl_server_start": [sz, d, ctypes.c_longlong, i, i, ctypes.POINTER(vp)],
         "msl_server_submit": [vp, i, i, i, i, vp, ctypes.POINTER(ctypes.c_longlong)],
         "msl_server_wait": [vp, ctypes.c_longlong, d],
@@ -181,6 +187,23 @@ class Batch:
         check(load().msl_batch_get_grid(self.handle, i, out.ctypes.data, ctypes.byref(it), ctypes.byref(res)),
               "msl_batch_get_grid")
         return out, it.value, res.value
+
+    def checkpoint(self, path: str) -> None:
+        check(load().msl_batch_checkpoint(self.handle, os.fsencode(path)), "msl_batch_checkpoint")
+
+    @classmethod
+    def restore(cls, path: str, hbm_budget: int = 0) -> "Batch":
+        """A batch from a checkpoint file; solve() resumes every grid."""
+        h = ctypes.c_void_p()
+        check(load().msl_batch_restore(os.fsencode(path), hbm_budget, ctypes.byref(h)), "msl_batch_restore")
+        with open(path, "rb") as f:
+            head = np.frombuffer(f.read(16)[8:], np.int32)
+            recs = np.frombuffer(f.read(32 * int(head[1])), np.int32).reshape(-1, 8)
+        b = cls.__new__(cls)
+        b.shapes = [(int(r), int(c)) for r, c in recs[:, :2]]
+        b.storage = int(head[0])
+        b.handle = h
+        return b
 
     def info(self):
         n, res, tiles, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong(), ctypes.c_size_t()
@@ -387,6 +410,56 @@ def fold_absdiff_max(a: DeviceArray, b: DeviceArray) -> float:
     r = ctypes.c_double()
     check(load().msl_fold_absdiff_max(a.code, a.ptr, b.ptr, a.size, ctypes.byref(r)), "msl_fold_absdiff_max")
     return r.value
+
+
+def fold_rows(op: int, m: DeviceArray, threads_per_block: int = 1024) -> DeviceArray:
+    """Per-row fold of a 2-D array (DM::reduceRows); returns a device vector."""
+    rows, cols = m.shape
+    out = DeviceArray((rows,), m.dtype)
+    check(load().msl_fold_rows(m.code, op, m.ptr, rows, cols, threads_per_block, out.ptr), "msl_fold_rows")
+    return out
+
+
+def fold_cols(op: int, m: DeviceArray) -> DeviceArray:
+    rows, cols = m.shape
+    out = DeviceArray((cols,), m.dtype)
+    check(load().msl_fold_cols(m.code, op, m.ptr, rows, cols, out.ptr), "msl_fold_cols")
+    return out
+
+
+def zip_rows(op: int, m: DeviceArray, v: DeviceArray, out: DeviceArray) -> None:
+    rows, cols = m.shape
+    check(load().msl_zip_rows(m.code, op, m.ptr, v.ptr, out.ptr, rows, cols), "msl_zip_rows")
+
+
+def rotate_rows(m: DeviceArray, out: DeviceArray, a: int) -> None:
+    rows, cols = m.shape
+    check(load().msl_rotate_rows(m.code, m.ptr, out.ptr, rows, cols, int(a)), "msl_rotate_rows")
+
+
+def rotate_cols(m: DeviceArray, out: DeviceArray, a: int) -> None:
+    rows, cols = m.shape
+    check(load().msl_rotate_cols(m.code, m.ptr, out.ptr, rows, cols, int(a)), "msl_rotate_cols")
+
+
+def set_column(m: DeviceArray, v: DeviceArray, col: int) -> None:
+    rows, cols = m.shape
+    check(load().msl_set_column(m.code, m.ptr, v.ptr, rows, cols, int(col)), "msl_set_column")
+
+
+def _grid_dims(shape):
+    return (1, *shape) if len(shape) == 2 else tuple(shape)
+
+
+def grid_dump_text(path: str, x: DeviceArray) -> None:
+    """Append a 2-D or 3-D device grid to `path` in the `;`-separated text format."""
+    d, r, c = _grid_dims(x.shape)
+    check(load().msl_grid_dump_text(os.fsencode(path), x.code, x.ptr, d, r, c), "msl_grid_dump_text")
+
+
+def grid_load_text(path: str, x: DeviceArray) -> None:
+    d, r, c = _grid_dims(x.shape)
+    check(load().msl_grid_load_text(os.fsencode(path), x.code, x.ptr, d, r, c), "msl_grid_load_text")
 
 
 def stencil2d(kind: int, x: DeviceArray, out: DeviceArray, radius: int, neutral: float) -> None:

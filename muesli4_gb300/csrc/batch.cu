@@ -5,6 +5,7 @@
 // No reference counterpart: the reference solves one DM at a time
 // (examples/jacobisolver.cpp:110-145).
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -39,6 +40,23 @@ struct Batch {
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
 };
+
+void clear_state(BatchGrid &g) {
+    g.cur = 0;
+    g.done = 0;
+    g.iters = 0;
+    g.residual = 0.0;
+    g.resid_bits = 0ull;
+}
+
+constexpr char kCheckpointMagic[8] = {'M', 'S', 'L', 'B', 'A', 'T', '0', '1'};
+struct CheckpointGrid {
+    int32_t rows, cols;
+    int64_t iters;
+    double residual;
+    int32_t done, pad;
+};
+static_assert(sizeof(CheckpointGrid) == 32, "checkpoint record layout");
 
 size_t grid_bytes(const Batch &b, int i) { return ((size_t)b.rows[i] * b.cols[i] * b.es + 255) / 256 * 256; }
 size_t resident_need(const Batch &b, int i) {
@@ -80,11 +98,16 @@ template <typename S>
 int solve_t(Batch &b, double tol, long long max_iters, int check_every, int depth) {
     auto &c = ctx();
     cudaStream_t st = c.stream;
-    // Reset the solve state of every grid (the data stay).
+    // Each grid continues from its own state: a grid set, reset or created
+    // starts at sweep 0; a grid that converged or ran out of sweeps in an
+    // earlier solve (or in a restored checkpoint) resumes from its sweep count
+    // and stops as soon as it is done under this call's tol and max_iters.
     for (auto &g : b.host) {
-        g.done = 0;
-        g.iters = 0;
-        g.residual = 0.0;
+        if (g.iters % check_every)
+            return rt::fail(MSL_ERR_INVALID_ARGUMENT,
+                            "msl_batch_solve: a grid stopped after %lld sweeps, not a multiple of check_every %d",
+                            g.iters, check_every);
+        g.done = g.iters >= max_iters || (g.iters > 0 && !(g.residual > tol));
         g.resid_bits = 0ull;
     }
     MSL_TRY_CUDA(cudaMemcpyAsync(b.dev, b.host.data(), b.host.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice, st),
@@ -261,7 +284,7 @@ int msl_batch_set_grid(void *batch, int index, const float *host_grid) {
         return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_set_grid: bad arguments");
     const size_t n = (size_t)b->rows[index] * b->cols[index];
     BatchGrid &gd = b->host[index];
-    gd.cur = 0;
+    clear_state(gd);
     if (b->storage == MSL_F32) {
         MSL_TRY_CUDA(cudaMemcpy(gd.buf[0], host_grid, n * 4, cudaMemcpyHostToDevice), "msl_batch_set_grid");
     } else {
@@ -320,8 +343,103 @@ int msl_batch_reset(void *batch) {
         const size_t n = (size_t)b->rows[i] * b->cols[i];
         MSL_TRY_CUDA(cudaMemcpyAsync(b->host[i].buf[0], b->init[i], n * b->es, cudaMemcpyDeviceToDevice, c.stream),
                      "msl_batch_reset");
-        b->host[i].cur = 0;
+        clear_state(b->host[i]);
     }
+    return MSL_OK;
+}
+
+// Checkpoint file: "MSLBAT01", int32 storage, int32 count, then per grid
+// {int32 rows, int32 cols, int64 sweeps, float64 residual, int32 done,
+// int32 0}, then per grid the latest iterate and the initial values, each
+// rows*cols elements of the storage type. Host byte order.
+int msl_batch_checkpoint(void *batch, const char *path) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    Batch *b = (Batch *)batch;
+    if (!b || !path) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_checkpoint: bad arguments");
+    MSL_TRY_CUDA(cudaStreamSynchronize(c.stream), "msl_batch_checkpoint");
+    FILE *f = fopen(path, "wb");
+    if (!f) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_checkpoint: cannot open %s", path);
+    bool ok = fwrite(kCheckpointMagic, 1, 8, f) == 8;
+    const int32_t head[2] = {b->storage, (int32_t)b->host.size()};
+    ok = ok && fwrite(head, sizeof head, 1, f) == 1;
+    for (size_t i = 0; ok && i < b->host.size(); i++) {
+        const BatchGrid &gd = b->host[i];
+        CheckpointGrid r{b->rows[i], b->cols[i], gd.iters, gd.residual, gd.done, 0};
+        ok = fwrite(&r, sizeof r, 1, f) == 1;
+    }
+    std::vector<char> h;
+    for (size_t i = 0; ok && i < b->host.size(); i++) {
+        const size_t bytes = (size_t)b->rows[i] * b->cols[i] * b->es;
+        h.resize(bytes);
+        const void *src[2] = {b->host[i].buf[b->host[i].cur], b->init[i]};
+        for (int k = 0; ok && k < 2; k++) {
+            cudaError_t e = cudaMemcpy(h.data(), src[k], bytes, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) {
+                fclose(f);
+                return rt::cuda_fail(e, "msl_batch_checkpoint");
+            }
+            ok = fwrite(h.data(), 1, bytes, f) == bytes;
+        }
+    }
+    ok = (fclose(f) == 0) && ok;
+    return ok ? MSL_OK : rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_checkpoint: write to %s failed", path);
+}
+
+int msl_batch_restore(const char *path, size_t hbm_budget, void **batch) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    if (int e = rt::require_init()) return e;
+    if (!path || !batch) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_restore: bad arguments");
+    *batch = nullptr;
+    FILE *f = fopen(path, "rb");
+    if (!f) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_restore: cannot open %s", path);
+    char magic[8];
+    int32_t head[2];
+    bool ok = fread(magic, 1, 8, f) == 8 && !memcmp(magic, kCheckpointMagic, 8) && fread(head, sizeof head, 1, f) == 1 &&
+              head[1] > 0 && head[1] <= (1 << 24);
+    std::vector<CheckpointGrid> recs;
+    if (ok) {
+        recs.resize(head[1]);
+        ok = fread(recs.data(), sizeof(CheckpointGrid), recs.size(), f) == recs.size();
+    }
+    std::vector<int> rows, cols;
+    for (size_t i = 0; ok && i < recs.size(); i++) {
+        ok = recs[i].rows > 0 && recs[i].cols > 0 && recs[i].iters >= 0;
+        rows.push_back(recs[i].rows);
+        cols.push_back(recs[i].cols);
+    }
+    if (!ok) {
+        fclose(f);
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_restore: %s is not a batch checkpoint", path);
+    }
+    void *handle = nullptr;
+    if (int e = msl_batch_create(head[0], head[1], rows.data(), cols.data(), hbm_budget, &handle)) {
+        fclose(f);
+        return e;
+    }
+    Batch *b = (Batch *)handle;
+    std::vector<char> h;
+    for (size_t i = 0; ok && i < recs.size(); i++) {
+        const size_t bytes = (size_t)rows[i] * cols[i] * b->es;
+        h.resize(bytes);
+        void *dst[2] = {b->host[i].buf[0], b->init[i]};
+        for (int k = 0; ok && k < 2; k++) {
+            ok = fread(h.data(), 1, bytes, f) == bytes;
+            if (ok && cudaMemcpy(dst[k], h.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) ok = false;
+        }
+        BatchGrid &gd = b->host[i];
+        clear_state(gd);
+        gd.iters = recs[i].iters;
+        gd.residual = recs[i].residual;
+        gd.done = recs[i].done;
+    }
+    fclose(f);
+    if (!ok) {
+        destroy(b);
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_restore: %s is truncated", path);
+    }
+    *batch = b;
     return MSL_OK;
 }
 

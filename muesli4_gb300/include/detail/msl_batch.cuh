@@ -61,6 +61,7 @@ __global__ void __launch_bounds__(kBatchResidentThreads)
     using T = typename Compute<S>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     BatchGrid &g = grids[list[blockIdx.x]];
+    if (g.done) return;  // converged or out of sweeps in an earlier solve
     const int rows = g.rows, cols = g.cols, n = rows * cols;
     const int n_pad = (n * (int)sizeof(S) + 127) / 128 * 128 / (int)sizeof(S);
     S *bufs[2] = {reinterpret_cast<S *>(smem_raw), reinterpret_cast<S *>(smem_raw) + n_pad};
@@ -81,8 +82,8 @@ __global__ void __launch_bounds__(kBatchResidentThreads)
     m.check_ = false;  // the Jacobi functor reads neighbours of inside cells only
     JacobiFn fn;
     int c = 0;
-    long long it = 0;
-    double res = 0.0;
+    long long it = g.iters;  // a multiple of check_every: checks stay on the same sweeps
+    double res = g.residual;
     __shared__ int s_stop;
     while (it < max_iters) {
         const long long k = min((long long)check_every, max_iters - it);
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(kBatchResidentThreads)
     for (int i = threadIdx.x; i < n; i += blockDim.x) dst_g[i] = bufs[c][i];
     if (threadIdx.x == 0) {
         g.cur = 0;
-        g.iters += it;
+        g.iters = it;
         g.residual = res;
         g.done = 1;
     }

@@ -196,12 +196,12 @@ MSL_DEV void tma_prefetch_desc(const void *tmap) {
 }
 
 // ---- warp helpers ----------------------------------------------------------------
-template <typename T> MSL_DEV T shfl_down(T v, int delta) {
+template <typename T> MSL_DEV T shfl_down(T v, int delta, int width = 32) {
     static_assert(sizeof(T) % 4 == 0, "shuffle of 4-byte multiples only");
     union { T t; int w[sizeof(T) / 4]; } u;
     u.t = v;
 #pragma unroll
-    for (int k = 0; k < (int)(sizeof(T) / 4); k++) u.w[k] = __shfl_down_sync(0xffffffffu, u.w[k], delta);
+    for (int k = 0; k < (int)(sizeof(T) / 4); k++) u.w[k] = __shfl_down_sync(0xffffffffu, u.w[k], delta, width);
     return u.t;
 }
 

@@ -3,6 +3,8 @@
 // f(row, col, ...); stencil functors f(view, x=col, y=row).
 #pragma once
 
+#include "da.h"
+#include "detail/msl_matrix.cuh"
 #include "detail/msl_stencil.cuh"
 #include "ds.h"
 
@@ -21,6 +23,69 @@ template <typename T, class F> struct PlmCall {
         else return f(y, x, &pl, m.width, m.height);
     }
 };
+
+// DM x DA broadcast zips (src/zip_kernels.cu:45-71): a[r][c] = f(r, c, a[r][c], ...).
+template <typename T, typename T2, typename T3, class F> struct ZipMAOp {  // ..., b[r][c], v[r]
+    T *a;
+    const T2 *b;
+    const T3 *v;
+    long long cols;
+    F f;
+    struct Row { long long base; T3 x; int r; };
+    __device__ __forceinline__ Row row(long long r) const { return Row{r * cols, v[r], (int)r}; }
+    __device__ __forceinline__ void operator()(const Row &w, long long, long long c) const {
+        const long long k = w.base + c;
+        a[k] = invoke(f, w.r, (int)c, a[k], b[k], w.x);
+    }
+};
+template <typename T, typename T3, class F> struct ZipAOp {  // ..., v[r]
+    T *a;
+    const T3 *v;
+    long long cols;
+    F f;
+    struct Row { long long base; T3 x; int r; };
+    __device__ __forceinline__ Row row(long long r) const { return Row{r * cols, v[r], (int)r}; }
+    __device__ __forceinline__ void operator()(const Row &w, long long, long long c) const {
+        const long long k = w.base + c;
+        a[k] = invoke(f, w.r, (int)c, a[k], w.x);
+    }
+};
+template <typename T, typename T2, typename T3, typename T4, class F> struct ZipAAAOp {  // ..., u[r], v[r], w[r]
+    T *a;
+    const T2 *u;
+    const T3 *v;
+    const T4 *w;
+    long long cols;
+    F f;
+    struct Row { long long base; T2 x; T3 y; T4 z; int r; };
+    __device__ __forceinline__ Row row(long long r) const { return Row{r * cols, u[r], v[r], w[r], (int)r}; }
+    __device__ __forceinline__ void operator()(const Row &q, long long, long long c) const {
+        const long long k = q.base + c;
+        a[k] = invoke(f, q.r, (int)c, a[k], q.x, q.y, q.z);
+    }
+};
+// crossZipIndexInPlace on the GPU (src/zip_kernels.cu:158-163): f(r, c, a, b)
+// with both containers' device pointers; the functor writes through them.
+template <typename T, typename T2, class F> struct CrossZipOp {
+    T *a;
+    T2 *b;
+    long long cols;
+    F f;
+    __device__ __forceinline__ int row(long long r) const { return (int)r; }
+    __device__ __forceinline__ void operator()(int r, long long, long long c) const { invoke(f, r, (int)c, a, b); }
+};
+// reducetwoColumns (src/dm.cpp:1729-1752): per row, s = 0, then
+// s = f(row[j], row[(j + 1) % cols], s) for j = 0 ... cols-1.
+template <typename T, typename R, class F>
+__global__ void reduce_two_columns_kernel(const T *in, R *out, long long rows, long long cols, F f) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += stride) {
+        const T *row = in + r * cols;
+        R s = R(0);
+        for (long long j = 0; j < cols; j++) s = invoke(f, row[j], row[j + 1 == cols ? 0 : j + 1], s);
+        out[r] = s;
+    }
+}
 }  // namespace detail
 
 template <typename T> class DM : public DS<T> {
@@ -115,6 +180,109 @@ template <typename T> class DM : public DS<T> {
         result.device_written();
     }
 
+    // ---- row / column skeletons ----
+    // c[r] = fold of row r with f, in the GPU build's row-fold order
+    // (src/dm.cpp:1677-1685, kernel src/fold_kernels.cu:215-294): lanes per row
+    // from Muesli::threads_per_block, element-seeded.
+    template <typename ReduceFunctor> void reduceRows(DA<T> &c, ReduceFunctor &f) {
+        static_assert(sizeof(T) % 4 == 0, "reduceRows shuffles 4-byte words");
+        if (c.getSize() != nrow) return throws(detail::SizeMismatchException());
+        const int tpb = Muesli::threads_per_block;
+        if (tpb < 1 || tpb > 1024 || (tpb & (tpb - 1))) return throws(detail::IllegalArgumentException());
+        this->ensure_device();
+        detail::launched(gpu::launch_fold_rows((const T *)this->d_, c.getDeviceData(), nrow, ncol, tpb,
+                                               detail::FoldCall<ReduceFunctor, T>{f}, stream(), sm_count()),
+                         "reduceRows");
+        c.device_written();
+    }
+    // c[r] = f(row[ncol-1], row[0], ... f(row[1], row[2], f(row[0], row[1], 0)))
+    // (src/dm.cpp:1729-1752), one device thread per row.
+    template <typename T2, typename ReduceFunctor> void reducetwoColumns(DA<T2> &c, ReduceFunctor &f) {
+        if (c.getSize() != nrow) return throws(detail::SizeMismatchException());
+        if (!nrow || !ncol) return;
+        this->ensure_device();
+        detail::reduce_two_columns_kernel<<<gpu::rows_blocks(nrow, 256, sm_count()), 256, 0, stream()>>>(
+            (const T *)this->d_, c.getDeviceData(), (long long)nrow, (long long)ncol, f);
+        detail::launched(cudaGetLastError(), "reducetwoColumns");
+        c.device_written();
+    }
+
+    // this[r][c] = f(r, c, this[r][c], b[r][c], v[r])  (src/dm.cpp:1757-1787)
+    template <typename T2, typename T3, typename ZipIndexFunctor>
+    void zipIndexInPlaceMA(DM<T2> &b, DA<T3> &v, ZipIndexFunctor &f) {
+        if (b.getSize() != this->n || v.getSize() < nrow) return throws(detail::NotSameSizeException());
+        this->ensure_device();
+        b.ensure_device();
+        v.ensure_device();
+        detail::ZipMAOp<T, T2, T3, ZipIndexFunctor> op{this->d_, b.getDeviceData(), v.getDeviceData(), ncol, f};
+        detail::launched(gpu::launch_row_cells(nrow, ncol, op, stream(), sm_count()), "zipIndexInPlaceMA");
+        this->device_written();
+    }
+    // this[r][c] = f(r, c, this[r][c], v[r])  (src/dm.cpp:1790-1812)
+    template <typename T3, typename ZipIndexFunctor> void zipIndexInPlaceA(DA<T3> &v, ZipIndexFunctor &f) {
+        if (v.getSize() < nrow) return throws(detail::NotSameSizeException());
+        this->ensure_device();
+        v.ensure_device();
+        detail::ZipAOp<T, T3, ZipIndexFunctor> op{this->d_, v.getDeviceData(), ncol, f};
+        detail::launched(gpu::launch_row_cells(nrow, ncol, op, stream(), sm_count()), "zipIndexInPlaceA");
+        this->device_written();
+    }
+    // this[r][c] = f(r, c, this[r][c], u[r], v[r], w[r])  (src/dm.cpp:1815-1853)
+    template <typename T2, typename T3, typename T4, typename ZipIndexFunctor>
+    void zipIndexInPlaceAAA(DA<T2> &u, DA<T3> &v, DA<T4> &w, ZipIndexFunctor &f) {
+        if (u.getSize() < nrow || v.getSize() < nrow || w.getSize() < nrow)
+            return throws(detail::NotSameSizeException());
+        this->ensure_device();
+        u.ensure_device();
+        v.ensure_device();
+        w.ensure_device();
+        detail::ZipAAAOp<T, T2, T3, T4, ZipIndexFunctor> op{this->d_, u.getDeviceData(), v.getDeviceData(),
+                                                             w.getDeviceData(), ncol, f};
+        detail::launched(gpu::launch_row_cells(nrow, ncol, op, stream(), sm_count()), "zipIndexInPlaceAAA");
+        this->device_written();
+    }
+    // f(r, c, this_data, b_data) for every cell (src/dm.cpp:505-536, GPU build):
+    // the functor reads and writes both matrices through the device pointers.
+    template <typename T2, typename ZipIndexFunctor> void crossZipIndexInPlace(DM<T2> &b, ZipIndexFunctor &f) {
+        this->ensure_device();
+        b.ensure_device();
+        detail::CrossZipOp<T, T2, ZipIndexFunctor> op{this->d_, b.getDeviceData(), ncol, f};
+        detail::launched(gpu::launch_row_cells(nrow, ncol, op, stream(), sm_count()), "crossZipIndexInPlace");
+        this->device_written();
+        b.device_written();
+    }
+
+    // Row k becomes row (k - a) mod nrow (src/dm.cpp:1345-1475); |a| > nrow is
+    // the reference's RotateRowManyNotImplementedException (matrix unchanged).
+    void rotateRows(int a) {
+        const long long howmuch = a < 0 ? -(long long)a : a;
+        if (a == 0 || howmuch == nrow || !this->n) return;
+        if (howmuch > nrow) return throws(detail::RotateRowManyNotImplementedException());
+        permute(a, true);
+    }
+    // Column j becomes column (j + a) mod ncol (src/dm.cpp:1483-1533).
+    void rotateCols(int a) {
+        if (!this->n || a % ncol == 0) return;
+        permute(a, false);
+    }
+    // this[r][col] = da[r]  (src/dm.cpp:1856-1879)
+    void setColumn(DA<T> &da, int col) {
+        if (col < 0 || col >= ncol) return throws(detail::IndexOutOfBoundsException());
+        if (da.getSize() != nrow) return throws(detail::SizeMismatchException());
+        this->ensure_device();
+        da.ensure_device();
+        gpu::set_column_kernel<<<gpu::rows_blocks(nrow, 256, sm_count()), 256, 0, stream()>>>(
+            this->d_, (const T *)da.getDeviceData(), (long long)nrow, (long long)ncol, (long long)col);
+        detail::launched(cudaGetLastError(), "setColumn");
+        this->device_written();
+    }
+    // One process holds every partition: broadcasting partition 0 leaves the
+    // data as it is; any other index is an IllegalPartitionException
+    // (src/dm.cpp:301-310).
+    void broadcastPartition(int partitionIndex) {
+        if (partitionIndex != 0) throws(detail::IllegalPartitionException());
+    }
+
     void show(const std::string &descr = std::string(), int limited = 0) {
         this->ensure_host();
         std::ostringstream s;
@@ -130,6 +298,27 @@ template <typename T> class DM : public DS<T> {
 
    private:
     int nrow = 0, ncol = 0;
+
+    // Rotation into a fresh device buffer, which then replaces the partition.
+    void permute(int a, bool rows) {
+        this->ensure_device();
+        T *tmp = nullptr;
+        if (!check_status(msl_alloc((void **)&tmp, this->bytes()), "rotate buffer")) return;
+        cudaError_t e;
+        if (rows) {
+            long long s = a % nrow;
+            if (s < 0) s += nrow;
+            e = gpu::launch_row_cells(nrow, ncol, gpu::RotateRowsOp<T>{this->d_, tmp, nrow, ncol, s}, stream(), sm_count());
+        } else {
+            long long s = a % ncol;
+            if (s < 0) s += ncol;
+            e = gpu::launch_row_cells(nrow, ncol, gpu::RotateColsOp<T>{this->d_, tmp, ncol, s}, stream(), sm_count());
+        }
+        detail::launched(e, rows ? "rotateRows" : "rotateCols");
+        msl_free(this->d_);  // waits for the rotation to finish
+        this->d_ = tmp;
+        this->device_written();
+    }
 };
 
 }  // namespace msl

@@ -99,6 +99,8 @@ MSL_DEFINE_EXCEPTION(InvalidCube, "InvalidCube")
 MSL_DEFINE_EXCEPTION(FeatureNotSupportedByDeviceException, "FeatureNotSupportedByDeviceException")
 MSL_DEFINE_EXCEPTION(InternalErrorException, "InternalErrorException")
 MSL_DEFINE_EXCEPTION(IllegalArgumentException, "IllegalArgumentException")
+MSL_DEFINE_EXCEPTION(IllegalPartitionException, "IllegalPartitionException")
+MSL_DEFINE_EXCEPTION(RotateRowManyNotImplementedException, "RotateRowManyNotImplementedException")
 #undef MSL_DEFINE_EXCEPTION
 }  // namespace detail
 

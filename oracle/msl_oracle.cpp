@@ -8,6 +8,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <fstream>
+#include <vector>
 
 #include "../include/msl_gb300.h"
 
@@ -374,6 +376,89 @@ double as_double(int dtype, const void *p, long long k) {
     }
 }
 
+
+// ---- DM row / column skeletons ------------------------------------------------
+template <typename T> T fold_op(int op, T a, T b) {
+    switch (op) {
+        case MSL_FOLD_SUM: return Ar<T>::add(a, b);
+        case MSL_FOLD_MAX: return a > b ? a : b;
+        default: return a < b ? a : b;  // MSL_FOLD_MIN
+    }
+}
+
+// DM::reduceRows on the GPU (src/dm.cpp:1677-1685): foldRowsKernel
+// (src/fold_kernels.cu:215-294) with one block of L threads per row,
+// L = nextPow2((cols + 1) / 2) below threads_per_block, else threads_per_block.
+// Thread t folds row[t], row[t + L], ... ; then sdata[t] = f(sdata[t], sdata[t + h])
+// for h = L/2 ... 1.
+template <typename T>
+void fold_rows_t(int op, const T *in, T *out, long long rows, long long cols, int tpb) {
+    long long lanes = tpb;
+    if (cols < tpb) {
+        lanes = 1;
+        while (lanes < (cols + 1) / 2) lanes <<= 1;
+    }
+    std::vector<T> v((size_t)lanes);
+    for (long long r = 0; r < rows; r++) {
+        const T *row = in + r * cols;
+        for (long long t = 0; t < lanes; t++) {
+            T acc = row[t];
+            for (long long c = t + lanes; c < cols; c += lanes) acc = fold_op(op, acc, row[c]);
+            v[(size_t)t] = acc;
+        }
+        for (long long h = lanes / 2; h > 0; h /= 2)
+            for (long long t = 0; t < h; t++) v[(size_t)t] = fold_op(op, v[(size_t)t], v[(size_t)(t + h)]);
+        out[r] = v[0];
+    }
+}
+
+template <typename T> void fold_cols_t(int op, const T *in, T *out, long long rows, long long cols) {
+    for (long long c = 0; c < cols; c++) {
+        T acc = in[c];
+        for (long long r = 1; r < rows; r++) acc = fold_op(op, acc, in[r * cols + c]);
+        out[c] = acc;
+    }
+}
+
+// DM::rotateRows (src/dm.cpp:1345-1475), one process: the `howmuch` rows that
+// wrap around go through a switch buffer, the others shift by `howmuch`.
+void rotate_rows_bytes(const unsigned char *in, unsigned char *out, long long rows, long long cols, long long a,
+                       size_t es) {
+    const bool negative = a < 0;
+    const long long howmuch = negative ? -a : a;
+    const size_t rb = (size_t)cols * es;
+    if (howmuch == rows || a == 0) {
+        std::memcpy(out, in, (size_t)rows * rb);
+        return;
+    }
+    std::vector<unsigned char> sw((size_t)howmuch * rb);
+    if (negative) std::memcpy(sw.data(), in, sw.size());
+    else std::memcpy(sw.data(), in + (size_t)(rows - howmuch) * rb, sw.size());
+    for (long long k = 0; k < rows; k++) {
+        const unsigned char *src;
+        if (negative) src = k >= rows - howmuch ? sw.data() + (size_t)(k - (rows - howmuch)) * rb : in + (size_t)(k + howmuch) * rb;
+        else src = k < howmuch ? sw.data() + (size_t)k * rb : in + (size_t)(k - howmuch) * rb;
+        std::memcpy(out + (size_t)k * rb, src, rb);
+    }
+}
+
+// DM::rotateCols (src/dm.cpp:1483-1533).
+void rotate_cols_bytes(const unsigned char *in, unsigned char *out, long long rows, long long cols, long long a,
+                       size_t es) {
+    long long howmuch = a < 0 ? -a : a;
+    if (howmuch >= cols) {
+        howmuch %= cols;
+        a %= cols;
+    }
+    for (long long i = 0; i < rows; i++)
+        for (long long j = 0; j < cols; j++) {
+            long long ce = j + a;
+            if (ce < 0) ce += cols;
+            if (ce >= cols) ce -= cols;
+            std::memcpy(out + (size_t)(i * cols + j) * es, in + (size_t)(i * cols + ce) * es, es);
+        }
+}
+
 }  // namespace
 
 extern "C" {
@@ -497,6 +582,97 @@ int oracle_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, i
     if (result_in_b) *result_in_b = (p == b);
     if (residual) oracle_fold_absdiff_max(dtype, p, q, (size_t)depth * rows * cols, residual);
     return 0;
+}
+
+int oracle_fold_rows(int dtype, int op, const void *in, long long rows, long long cols, int tpb, void *out) {
+    if (rows <= 0 || cols <= 0 || tpb < 1 || tpb > 1024 || (tpb & (tpb - 1))) return MSL_ERR_INVALID_ARGUMENT;
+    switch (dtype) {
+        case MSL_F32: fold_rows_t<float>(op, (const float *)in, (float *)out, rows, cols, tpb); return 0;
+        case MSL_F64: fold_rows_t<double>(op, (const double *)in, (double *)out, rows, cols, tpb); return 0;
+        case MSL_I32: fold_rows_t<int32_t>(op, (const int32_t *)in, (int32_t *)out, rows, cols, tpb); return 0;
+    }
+    return MSL_ERR_INVALID_ARGUMENT;
+}
+
+int oracle_fold_cols(int dtype, int op, const void *in, long long rows, long long cols, void *out) {
+    if (rows <= 0 || cols <= 0) return MSL_ERR_INVALID_ARGUMENT;
+    switch (dtype) {
+        case MSL_F32: fold_cols_t<float>(op, (const float *)in, (float *)out, rows, cols); return 0;
+        case MSL_F64: fold_cols_t<double>(op, (const double *)in, (double *)out, rows, cols); return 0;
+        case MSL_I32: fold_cols_t<int32_t>(op, (const int32_t *)in, (int32_t *)out, rows, cols); return 0;
+    }
+    return MSL_ERR_INVALID_ARGUMENT;
+}
+
+int oracle_zip_rows(int dtype, int op, const void *m, const void *v, void *out, long long rows, long long cols) {
+    if (rows <= 0 || cols <= 0) return MSL_ERR_INVALID_ARGUMENT;
+    for (long long r = 0; r < rows; r++)
+        for (long long c = 0; c < cols; c++) {
+            const long long k = r * cols + c;
+            switch (dtype) {
+                case MSL_F32: ((float *)out)[k] = zip_op<float>(op, ((const float *)m)[k], ((const float *)v)[r]); break;
+                case MSL_F64: ((double *)out)[k] = zip_op<double>(op, ((const double *)m)[k], ((const double *)v)[r]); break;
+                case MSL_I32: ((int32_t *)out)[k] = zip_op<int32_t>(op, ((const int32_t *)m)[k], ((const int32_t *)v)[r]); break;
+                default: return MSL_ERR_INVALID_ARGUMENT;
+            }
+        }
+    return 0;
+}
+
+int oracle_rotate_rows(int dtype, const void *in, void *out, long long rows, long long cols, long long a) {
+    const size_t es = dsize(dtype);
+    if (rows <= 0 || cols <= 0 || es == 0) return MSL_ERR_INVALID_ARGUMENT;
+    if ((a < 0 ? -a : a) > rows) return MSL_ERR_NOT_IMPLEMENTED;  // RotateRowManyNotImplementedException
+    rotate_rows_bytes((const unsigned char *)in, (unsigned char *)out, rows, cols, a, es);
+    return 0;
+}
+
+int oracle_rotate_cols(int dtype, const void *in, void *out, long long rows, long long cols, long long a) {
+    const size_t es = dsize(dtype);
+    if (rows <= 0 || cols <= 0 || es == 0) return MSL_ERR_INVALID_ARGUMENT;
+    rotate_cols_bytes((const unsigned char *)in, (unsigned char *)out, rows, cols, a, es);
+    return 0;
+}
+
+// DM::setColumn on one process (src/dm.cpp:1874-1877).
+int oracle_set_column(int dtype, void *dm, const void *da, long long rows, long long cols, long long col) {
+    const size_t es = dsize(dtype);
+    if (rows <= 0 || cols <= 0 || es == 0) return MSL_ERR_INVALID_ARGUMENT;
+    if (col < 0 || col >= cols) return MSL_ERR_INVALID_ARGUMENT;
+    for (long long i = 0; i < rows; i++)
+        std::memcpy((unsigned char *)dm + (size_t)(i * cols + col) * es, (const unsigned char *)da + (size_t)i * es, es);
+    return 0;
+}
+
+// The result dumps of examples/heatdiffusion.cpp:99-114 (2-D) and :156-170
+// (3-D), generalised from size^2 / size^3 to rows x cols / depth x rows x cols:
+// an std::ofstream in append mode, `out << value << ";"`, "\n" per line.
+int oracle_dump_text(const char *path, int dtype, const void *grid, int depth, int rows, int cols) {
+    if (!path || depth < 1 || rows < 1 || cols < 1 || dsize(dtype) == 0) return MSL_ERR_INVALID_ARGUMENT;
+    std::ofstream out(path, std::ios::app | std::ios::binary);
+    if (!out) return MSL_ERR_INVALID_ARGUMENT;
+    auto put = [&](long long index) {
+        switch (dtype) {
+            case MSL_F32: out << ((const float *)grid)[index]; break;
+            case MSL_F64: out << ((const double *)grid)[index]; break;
+            case MSL_I32: out << ((const int32_t *)grid)[index]; break;
+            default: out << to_f(((const bf16 *)grid)[index]); break;
+        }
+        out << ";";
+    };
+    if (depth == 1) {
+        for (int x = 0; x < rows; x++) {
+            for (int y = 0; y < cols; y++) put(y + (long long)cols * x);
+            out << "\n";
+        }
+    } else {
+        for (int x = 0; x < cols; x++)
+            for (int y = 0; y < rows; y++) {
+                for (int z = 0; z < depth; z++) put(x + (long long)cols * y + (long long)cols * rows * z);
+                out << "\n";
+            }
+    }
+    return out.good() ? 0 : MSL_ERR_INVALID_ARGUMENT;
 }
 
 }  // extern "C"

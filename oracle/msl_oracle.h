@@ -40,6 +40,17 @@ int oracle_stencil3d(int dtype, int kind, const void *in, void *out, int depth, 
                      int radius, double neutral);
 int oracle_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int rows, int cols,
                              int radius, double neutral, int iters, double *residual, int *result_in_b);
+/* DM row / column skeletons: reduceRows (GPU row-fold order), column folds,
+ * matrix x per-row-vector zips, rotateRows, rotateCols, setColumn. */
+int oracle_fold_rows(int dtype, int op, const void *in, long long rows, long long cols, int threads_per_block,
+                     void *out);
+int oracle_fold_cols(int dtype, int op, const void *in, long long rows, long long cols, void *out);
+int oracle_zip_rows(int dtype, int op, const void *m, const void *v, void *out, long long rows, long long cols);
+int oracle_rotate_rows(int dtype, const void *in, void *out, long long rows, long long cols, long long a);
+int oracle_rotate_cols(int dtype, const void *in, void *out, long long rows, long long cols, long long a);
+int oracle_set_column(int dtype, void *dm, const void *da, long long rows, long long cols, long long col);
+/* Text dump of a grid in the examples' `;`-separated format (appends). */
+int oracle_dump_text(const char *path, int dtype, const void *grid, int depth, int rows, int cols);
 
 #ifdef __cplusplus
 }

@@ -50,6 +50,14 @@ def lib():
         L.oracle_stencil2d_iterate.argtypes = [i, i, vp, vp, i, i, i, d, i, dp, ip]
         L.oracle_stencil3d.argtypes = [i, i, vp, vp, i, i, i, i, d]
         L.oracle_stencil3d_iterate.argtypes = [i, i, vp, vp, i, i, i, i, d, i, dp, ip]
+        ll = ctypes.c_longlong
+        L.oracle_fold_rows.argtypes = [i, i, vp, ll, ll, i, vp]
+        L.oracle_fold_cols.argtypes = [i, i, vp, ll, ll, vp]
+        L.oracle_zip_rows.argtypes = [i, i, vp, vp, vp, ll, ll]
+        L.oracle_rotate_rows.argtypes = [i, vp, vp, ll, ll, ll]
+        L.oracle_rotate_cols.argtypes = [i, vp, vp, ll, ll, ll]
+        L.oracle_set_column.argtypes = [i, vp, vp, ll, ll, ll]
+        L.oracle_dump_text.argtypes = [ctypes.c_char_p, i, vp, i, i, i]
         _lib = L
     return _lib
 
@@ -180,3 +188,69 @@ def to_bf16(x: np.ndarray) -> np.ndarray:
 
 def from_bf16(h: np.ndarray) -> np.ndarray:
     return (h.astype(np.uint32) << 16).view(np.float32)
+
+
+# ---- DM row / column skeletons ------------------------------------------------
+def fold_rows(op: int, m: np.ndarray, threads_per_block: int = 1024) -> np.ndarray:
+    m = np.ascontiguousarray(m)
+    out = np.empty(m.shape[0], m.dtype)
+    _check(lib().oracle_fold_rows(dtype_code(m), op, _ptr(m), m.shape[0], m.shape[1], threads_per_block, _ptr(out)),
+           "fold_rows")
+    return out
+
+
+def fold_cols(op: int, m: np.ndarray) -> np.ndarray:
+    m = np.ascontiguousarray(m)
+    out = np.empty(m.shape[1], m.dtype)
+    _check(lib().oracle_fold_cols(dtype_code(m), op, _ptr(m), m.shape[0], m.shape[1], _ptr(out)), "fold_cols")
+    return out
+
+
+def zip_rows(op: int, m: np.ndarray, v: np.ndarray) -> np.ndarray:
+    m, v = np.ascontiguousarray(m), np.ascontiguousarray(v, dtype=m.dtype)
+    out = np.empty_like(m)
+    _check(lib().oracle_zip_rows(dtype_code(m), op, _ptr(m), _ptr(v), _ptr(out), m.shape[0], m.shape[1]), "zip_rows")
+    return out
+
+
+def rotate_rows(m: np.ndarray, a: int) -> np.ndarray:
+    """Returns the rotated copy; raises on |a| > rows like the reference's exception."""
+    m = np.ascontiguousarray(m)
+    out = np.empty_like(m)
+    _check(lib().oracle_rotate_rows(dtype_code(m), _ptr(m), _ptr(out), m.shape[0], m.shape[1], int(a)), "rotate_rows")
+    return out
+
+
+def rotate_cols(m: np.ndarray, a: int) -> np.ndarray:
+    m = np.ascontiguousarray(m)
+    out = np.empty_like(m)
+    _check(lib().oracle_rotate_cols(dtype_code(m), _ptr(m), _ptr(out), m.shape[0], m.shape[1], int(a)), "rotate_cols")
+    return out
+
+
+def set_column(m: np.ndarray, v: np.ndarray, col: int) -> np.ndarray:
+    out = np.array(m, copy=True, order="C")
+    v = np.ascontiguousarray(v, dtype=m.dtype)
+    _check(lib().oracle_set_column(dtype_code(out), _ptr(out), _ptr(v), out.shape[0], out.shape[1], int(col)),
+           "set_column")
+    return out
+
+
+def reduce_two_columns_dot(m: np.ndarray) -> np.ndarray:
+    """DM::reducetwoColumns (src/dm.cpp:1729-1752) with f(x, y, s) = s + x*y:
+    per row, s = 0, then s = f(row[j], row[(j + 1) % cols], s) for j = 0 ... cols-1,
+    one float32 rounding per operation."""
+    m = np.ascontiguousarray(m, dtype=np.float32)
+    s = np.zeros(m.shape[0], np.float32)
+    cols = m.shape[1]
+    for j in range(cols):
+        s = s + m[:, j] * m[:, (j + 1) % cols]
+    return s
+
+
+def dump_text(path: str, grid: np.ndarray) -> None:
+    """Append `grid` (2-D rows x cols or 3-D depth x rows x cols) to `path` in the
+    reference examples' `;`-separated text format."""
+    g = np.ascontiguousarray(grid)
+    d, r, c = (1, *g.shape) if g.ndim == 2 else g.shape
+    _check(lib().oracle_dump_text(os.fsencode(path), dtype_code(g), _ptr(g), d, r, c), "dump_text")

@@ -77,6 +77,10 @@ struct AbsDiff : public Functor2<float, float, float> {
         return d;
     }
 };
+// reducetwoColumns functor: (x, y, s) -> s + x*y  (two roundings)
+struct DotNext : public Functor3<float, float, float, float> {
+    MSL_USERFUNC float operator()(float x, float y, float s) const override { return s + x * y; }
+};
 struct XorIndex : public Functor2<int, int, int> {  // (i, x) -> x ^ (i & 1023)
     MSL_USERFUNC int operator()(int i, int x) const override { return x ^ (i & 1023); }
 };
@@ -401,6 +405,56 @@ int main(int argc, char **argv) {
         std::memcpy(o.data(), p->getLocalPartition(), n * sizeof(float));
         o[n] = res;
         store(out, o.data(), n + 1);
+    } else if (op == "dm_reduce_rows_sum_i32" || op == "dm_reduce_rows_max_f32") {  // rows cols
+        omp_set_num_threads(1);  // the CPU build folds each row with a racy omp loop
+        int rows = (int)I(0), cols = (int)I(1);
+        size_t n = (size_t)rows * cols;
+        if (op == "dm_reduce_rows_sum_i32") {
+            std::vector<int> x = load<int>(ins.at(0), n);
+            DM<int> a(rows, cols, 0, true);
+            DA<int> c(rows, 0);
+            a.setLocalPartition(x.data());
+            SumI f;
+            a.reduceRows(c, f);
+            store(out, c.getLocalPartition(), rows);
+        } else {
+            std::vector<float> x = load<float>(ins.at(0), n);
+            DM<float> a(rows, cols, 0.0f, true);
+            DA<float> c(rows, 0.0f);
+            a.setLocalPartition(x.data());
+            MaxF f;
+            a.reduceRows(c, f);
+            store(out, c.getLocalPartition(), rows);
+        }
+    } else if (op == "dm_reduce_two_columns") {  // rows cols
+        int rows = (int)I(0), cols = (int)I(1);
+        size_t n = (size_t)rows * cols;
+        std::vector<float> x = load<float>(ins.at(0), n);
+        DM<float> a(rows, cols, 0.0f, true);
+        DA<float> c(rows, 0.0f);
+        a.setLocalPartition(x.data());
+        DotNext f;
+        a.reducetwoColumns(c, f);
+        store(out, c.getLocalPartition(), rows);
+    } else if (op == "dm_rotate_rows" || op == "dm_rotate_cols") {  // rows cols a
+        int rows = (int)I(0), cols = (int)I(1), a = (int)I(2);
+        size_t n = (size_t)rows * cols;
+        std::vector<int> x = load<int>(ins.at(0), n);
+        DM<int> m(rows, cols, 0, true);
+        m.setLocalPartition(x.data());
+        if (op == "dm_rotate_rows") m.rotateRows(a);
+        else m.rotateCols(a);
+        store(out, m.getLocalPartition(), n);
+    } else if (op == "dm_set_column") {  // rows cols col
+        int rows = (int)I(0), cols = (int)I(1), col = (int)I(2);
+        size_t n = (size_t)rows * cols;
+        std::vector<float> x = load<float>(ins.at(0), n), v = load<float>(ins.at(1), rows);
+        DM<float> m(rows, cols, 0.0f, true);
+        DA<float> d(rows, 0.0f);
+        m.setLocalPartition(x.data());
+        d.setLocalPartition(v.data());
+        m.setColumn(d, col);
+        store(out, m.getLocalPartition(), n);
     } else {
         std::fprintf(stderr, "ref_harness: unknown op %s\n", op.c_str());
         return 2;

@@ -100,6 +100,48 @@ class MaxF : public Functor2<float, float, float> {
     MSL_USERFUNC float operator()(float x, float y) const override { return x > y ? x : y; }
 };
 
+// Row / column skeletons and the DM x DA zips (functors of the ACO examples' shape).
+class DotNext : public Functor3<float, float, float, float> {  // reducetwoColumns: s + x*y
+   public:
+    MSL_USERFUNC float operator()(float x, float y, float s) const override { return s + x * y; }
+};
+class ZipMA : public Functor5<int, int, int, int, int, int> {  // (r, c, a, b[r][c], v[r])
+   public:
+    MSL_USERFUNC int operator()(int r, int c, int a, int b, int v) const override {
+        return 1000 * r + 7 * c + 2 * a - 3 * b + 5 * v;
+    }
+};
+class ZipA : public Functor4<int, int, int, int, int> {  // (r, c, a, v[r])
+   public:
+    MSL_USERFUNC int operator()(int r, int c, int a, int v) const override { return 1000 * r + 7 * c - a + 11 * v; }
+};
+class ZipAAA : public Functor6<int, int, int, int, int, int, int> {  // (r, c, a, u[r], v[r], w[r])
+   public:
+    MSL_USERFUNC int operator()(int r, int c, int a, int u, int v, int w) const override {
+        return 1000 * r + 7 * c + a - 2 * u + 3 * v - 5 * w;
+    }
+};
+// crossZipIndexInPlace: a[r][c] = b[c][r] + a[r][c] on a square matrix (the
+// functor indexes both matrices through their device pointers).
+struct CrossT {
+    int n;
+    MSL_USERFUNC void operator()(int r, int c, int *a, int *b) const { a[r * n + c] = b[c * n + r] + a[r * n + c]; }
+};
+// mapIndexInPlaceDMRows: this[i] = i + sum of row i - this[i]
+struct RowSum {
+    int cols;
+    MSL_USERFUNC int operator()(int i, int *row, int x) const {
+        int s = 0;
+        for (int k = 0; k < cols; k++) s += row[k];
+        return i + s - x;
+    }
+};
+// zipIndexInPlaceDMRows: this[i] = row[i % cols] * b[i] + this[i] + i
+struct RowPick {
+    int cols;
+    MSL_USERFUNC int operator()(int i, int *row, int b, int x) const { return row[i % cols] * b + x + i; }
+};
+
 // ---- stencil functions -----------------------------------------------------------
 MSL_USERFUNC float jacobi5(const NPLMatrix<float> &m, int x, int y) {
     if (x == 0 || y == 0 || x == m.width - 1 || y == m.height - 1) return m(x, y);
@@ -381,6 +423,91 @@ int fe_dc_index(const int *in, const int *in2, int depth, int rows, int cols, in
     DcZipIdx g;
     a.zipIndexInPlace(b, g);
     std::memcpy(zipped, a.gather(), sizeof(int) * depth * rows * cols);
+    return 0;
+}
+
+// DM::reduceRows with a Functor2 class (int) or a lambda (float) and a given
+// threads-per-block setting.
+int fe_reduce_rows_i32(const int *in, int rows, int cols, int tpb, int *out) {
+    DM<int> a(rows, cols, 0, true);
+    DA<int> c(rows, 0);
+    a.setLocalPartition(const_cast<int *>(in));
+    const int keep = Muesli::threads_per_block;
+    setThreadsPerBlock(tpb);
+    Sum f;
+    a.reduceRows(c, f);
+    setThreadsPerBlock(keep);
+    std::memcpy(out, c.gather(), sizeof(int) * rows);
+    return 0;
+}
+int fe_reduce_rows_f32(const float *in, int rows, int cols, int tpb, int op, float *out) {
+    DM<float> a(rows, cols, 0.0f, true);
+    DA<float> c(rows, 0.0f);
+    a.setLocalPartition(const_cast<float *>(in));
+    const int keep = Muesli::threads_per_block;
+    setThreadsPerBlock(tpb);
+    if (op == 0) {
+        auto plus = [] MSL_USERFUNC(float x, float y) { return x + y; };
+        a.reduceRows(c, plus);
+    } else {
+        MaxF mx;
+        a.reduceRows(c, mx);
+    }
+    setThreadsPerBlock(keep);
+    std::memcpy(out, c.gather(), sizeof(float) * rows);
+    return 0;
+}
+int fe_reduce_two_columns(const float *in, int rows, int cols, float *out) {
+    DM<float> a(rows, cols, 0.0f, true);
+    DA<float> c(rows, 0.0f);
+    a.setLocalPartition(const_cast<float *>(in));
+    DotNext f;
+    a.reducetwoColumns(c, f);
+    std::memcpy(out, c.gather(), sizeof(float) * rows);
+    return 0;
+}
+// which: 0 rotateRows, 1 rotateCols; the matrix is rotated in place.
+int fe_rotate(const int *in, int rows, int cols, int a, int which, int *out) {
+    DM<int> m(rows, cols, 0, true);
+    m.setLocalPartition(const_cast<int *>(in));
+    if (which == 0) m.rotateRows(a);
+    else m.rotateCols(a);
+    std::memcpy(out, m.gather(), sizeof(int) * rows * cols);
+    return 0;
+}
+int fe_set_column(const float *in, const float *v, int rows, int cols, int col, float *out) {
+    DM<float> m(rows, cols, 0.0f, true);
+    DA<float> d(rows, 0.0f);
+    m.setLocalPartition(const_cast<float *>(in));
+    d.setLocalPartition(const_cast<float *>(v));
+    m.setColumn(d, col);
+    m.broadcastPartition(0);
+    std::memcpy(out, m.gather(), sizeof(float) * rows * cols);
+    return 0;
+}
+// kind: 0 zipIndexInPlaceMA(b, u), 1 zipIndexInPlaceA(u), 2 zipIndexInPlaceAAA(u, v, w),
+// 3 crossZipIndexInPlace(b) (square), 4 DA::mapIndexInPlaceDMRows (on u, rows = a),
+// 5 DA::zipIndexInPlaceDMRows (on u, b-vector = v, rows = a).
+int fe_dm_da(int kind, const int *a, const int *b, const int *u, const int *v, const int *w, int rows, int cols,
+             int *out) {
+    DM<int> ma(rows, cols, 0, true), mb(rows, cols, 0, true);
+    DA<int> du(rows, 0), dv(rows, 0), dw(rows, 0);
+    ma.setLocalPartition(const_cast<int *>(a));
+    mb.setLocalPartition(const_cast<int *>(b));
+    du.setLocalPartition(const_cast<int *>(u));
+    dv.setLocalPartition(const_cast<int *>(v));
+    dw.setLocalPartition(const_cast<int *>(w));
+    if (kind == 0) { ZipMA f; ma.zipIndexInPlaceMA(mb, du, f); }
+    else if (kind == 1) { ZipA f; ma.zipIndexInPlaceA(du, f); }
+    else if (kind == 2) { ZipAAA f; ma.zipIndexInPlaceAAA(du, dv, dw, f); }
+    else if (kind == 3) { CrossT f{cols}; ma.crossZipIndexInPlace(mb, f); }
+    if (kind <= 3) {
+        std::memcpy(out, ma.gather(), sizeof(int) * rows * cols);
+        return 0;
+    }
+    if (kind == 4) { RowSum f{cols}; du.mapIndexInPlaceDMRows(ma, f); }
+    else { RowPick f{cols}; du.zipIndexInPlaceDMRows(dv, ma, f); }
+    std::memcpy(out, du.gather(), sizeof(int) * rows);
     return 0;
 }
 

@@ -123,6 +123,32 @@ def main():
     for r in (1, 2):
         save(f"dc_boxsum_r{r}", seed=57, ints=[9, 10, 11, r, 1], in0=cb,
              out=run("dc_boxsum", [9, 10, 11, r, 1], [cb], np.float32, cb.size))
+    # DM row / column skeletons: reduceRows (int sum with wrap-around; max over
+    # positive floats, where the CPU build's 0 seed is neutral), reducetwoColumns,
+    # rotateRows / rotateCols (both signs, |a| >= size), setColumn.
+    ri = rng(58).integers(-2**30, 2**30, (41, 77), dtype=np.int32)
+    save("dm_reduce_rows_sum_i32", seed=58, ints=[41, 77], in0=ri,
+         out=run("dm_reduce_rows_sum_i32", [41, 77], [ri], np.int32, 41))
+    wide = rng(59).integers(-1000, 1000, (5, 2500), dtype=np.int32)
+    save("dm_reduce_rows_sum_i32_wide", seed=59, ints=[5, 2500], in0=wide,
+         out=run("dm_reduce_rows_sum_i32", [5, 2500], [wide], np.int32, 5))
+    rf = rng(60).random((41, 77), dtype=np.float32)
+    save("dm_reduce_rows_max_f32", seed=60, ints=[41, 77], in0=rf,
+         out=run("dm_reduce_rows_max_f32", [41, 77], [rf], np.float32, 41))
+    tc = rng(61).uniform(-1, 1, (23, 19)).astype(np.float32)
+    save("dm_reduce_two_columns", seed=61, ints=[23, 19], in0=tc,
+         out=run("dm_reduce_two_columns", [23, 19], [tc], np.float32, 23))
+    rot = rng(62).integers(-1000, 1000, (11, 13), dtype=np.int32)
+    for tag, a in (("p2", 2), ("m3", -3), ("p11", 11), ("p12", 12)):
+        save(f"dm_rotate_rows_{tag}", seed=62, ints=[11, 13, a], in0=rot,
+             out=run("dm_rotate_rows", [11, 13, a], [rot], np.int32, rot.size))
+    for tag, a in (("p3", 3), ("m5", -5), ("m30", -30), ("p13", 13)):
+        save(f"dm_rotate_cols_{tag}", seed=62, ints=[11, 13, a], in0=rot,
+             out=run("dm_rotate_cols", [11, 13, a], [rot], np.int32, rot.size))
+    sc = rng(63).random((17, 9), dtype=np.float32)
+    sv = rng(64).random(17, dtype=np.float32)
+    save("dm_set_column", seed=[63, 64], ints=[17, 9, 4], in0=sc, in1=sv,
+         out=run("dm_set_column", [17, 9, 4], [sc, sv], np.float32, sc.size))
     print("golden fixtures written to", HERE)
 
 

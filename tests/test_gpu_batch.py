@@ -108,3 +108,62 @@ def test_batch_reset_restores_initial_values(gpu):
         again = b.get_grid(i)
         assert again[1:] == first[i][1:] and np.array_equal(again[0], first[i][0])
     b.close()
+
+
+@pytest.mark.parametrize("storage", ["f32", "bf16"])
+def test_checkpoint_and_resume_equal_one_solve(gpu, storage, tmp_path):
+    """Solve 400 sweeps, checkpoint to a file, restore into a new batch and
+    continue to 1200: every grid equals one uninterrupted 1200-sweep solve
+    (same sweep count, residual and bits). A second solve on the same batch
+    continues the same way."""
+    tol, check_every = 1e-4, 100
+    grids = [W.jacobi_grid(r, c, 500 + i) for i, (r, c) in enumerate(SHAPES)]
+    st = gpu.MSL_F32 if storage == "f32" else gpu.MSL_BF16
+    whole = gpu.Batch(SHAPES, storage=st)
+    part = gpu.Batch(SHAPES, storage=st)
+    for i, g in enumerate(grids):
+        whole.set_grid(i, g)
+        part.set_grid(i, g)
+    whole.solve(tol, 1200, check_every, 2)
+    part.solve(tol, 400, check_every, 2)
+    assert all(part.get_grid(i)[1] <= 400 for i in range(len(SHAPES)))
+    path = str(tmp_path / "batch.ckpt")
+    part.checkpoint(path)
+    resumed = gpu.Batch.restore(path)
+    assert resumed.shapes == SHAPES
+    resumed.solve(tol, 1200, check_every, 5)  # another temporal depth: same sweeps
+    part.solve(tol, 1200, check_every, 2)
+    for i in range(len(SHAPES)):
+        want, want_it, want_res = whole.get_grid(i)
+        for b in (resumed, part):
+            got, it, res = b.get_grid(i)
+            assert it == want_it and res == want_res, (SHAPES[i], it, want_it)
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), SHAPES[i]
+    resumed.reset()  # the initial values travel in the checkpoint too
+    resumed.solve(tol, 1200, check_every, 2)
+    for i in range(len(SHAPES)):
+        assert np.array_equal(resumed.get_grid(i)[0].view(np.uint32), whole.get_grid(i)[0].view(np.uint32))
+    for b in (whole, part, resumed):
+        b.close()
+
+
+def test_restore_rejects_bad_files(gpu, tmp_path):
+    bad = tmp_path / "bad.ckpt"
+    bad.write_bytes(b"not a checkpoint")
+    with pytest.raises(gpu.MslError) as e:
+        gpu.Batch.restore(str(bad))
+    assert e.value.code == gpu.MSL_ERR_INVALID_ARGUMENT
+    b = gpu.Batch([(64, 64), (300, 300)])
+    b.set_grid(0, W.jacobi_grid(64, 64, 1))
+    b.set_grid(1, W.jacobi_grid(300, 300, 2))
+    good = tmp_path / "good.ckpt"
+    b.checkpoint(str(good))
+    data = good.read_bytes()
+    trunc = tmp_path / "trunc.ckpt"
+    trunc.write_bytes(data[:-100])
+    with pytest.raises(gpu.MslError):
+        gpu.Batch.restore(str(trunc))
+    with pytest.raises(gpu.MslError) as e:
+        gpu.Batch.restore(str(good), hbm_budget=1 << 16)
+    assert e.value.code == gpu.MSL_ERR_BUDGET
+    b.close()

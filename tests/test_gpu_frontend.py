@@ -143,3 +143,106 @@ def test_dm_and_dc_index_functors_pin_argument_order(fe):
     assert fe.fe_dc_index(ptr(a3), ptr(b3), 5, 7, 11, ptr(m3), ptr(z3)) == 0
     assert np.array_equal(m3, O.map_index(0, a3, (7, 1000, 100000, -1)))
     assert np.array_equal(z3, O.zip_index(0, a3, b3, (7, 1000, 100000, 2, -3)))
+
+
+# ---- row / column skeletons and the DM x DA zips ------------------------------------
+GOLDEN = os.path.join(HERE, "golden")
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (5, 3), (41, 77), (9, 129), (3, 4097), (1000, 7)],
+                         ids=lambda s: f"{s[0]}x{s[1]}")
+@pytest.mark.parametrize("tpb", [1024, 256, 32, 4])
+def test_reduce_rows(fe, shape, tpb):
+    rows, cols = shape
+    g = np.random.default_rng(rows + cols)
+    xi = g.integers(-2**31, 2**31, shape, dtype=np.int64).astype(np.int32)
+    out = np.empty(rows, np.int32)
+    assert fe.fe_reduce_rows_i32(ptr(xi), rows, cols, tpb, ptr(out)) == 0
+    assert np.array_equal(out, O.fold_rows(0, xi, tpb))
+    xf = g.uniform(-1, 1, shape).astype(np.float32)
+    outf = np.empty(rows, np.float32)
+    for op in (0, 1):  # lambda sum, Functor2 max
+        assert fe.fe_reduce_rows_f32(ptr(xf), rows, cols, tpb, op, ptr(outf)) == 0
+        assert np.array_equal(outf.view(np.uint32), O.fold_rows(op, xf, tpb).view(np.uint32))
+
+
+def test_reduce_rows_golden(fe):
+    for name, fn, dt in (("dm_reduce_rows_sum_i32", fe.fe_reduce_rows_i32, np.int32),
+                         ("dm_reduce_rows_sum_i32_wide", fe.fe_reduce_rows_i32, np.int32)):
+        f = np.load(os.path.join(GOLDEN, name + ".npz"))
+        x = np.ascontiguousarray(f["in0"])
+        out = np.empty(x.shape[0], dt)
+        assert fn(ptr(x), x.shape[0], x.shape[1], 1024, ptr(out)) == 0
+        assert np.array_equal(out, f["out"])
+    f = np.load(os.path.join(GOLDEN, "dm_reduce_rows_max_f32.npz"))
+    x = np.ascontiguousarray(f["in0"])
+    out = np.empty(x.shape[0], np.float32)
+    assert fe.fe_reduce_rows_f32(ptr(x), x.shape[0], x.shape[1], 1024, 1, ptr(out)) == 0
+    assert np.array_equal(out, f["out"])
+
+
+def test_reduce_two_columns_golden_and_oracle(fe):
+    f = np.load(os.path.join(GOLDEN, "dm_reduce_two_columns.npz"))
+    x = np.ascontiguousarray(f["in0"])
+    out = np.empty(x.shape[0], np.float32)
+    assert fe.fe_reduce_two_columns(ptr(x), x.shape[0], x.shape[1], ptr(out)) == 0
+    assert np.array_equal(out.view(np.uint32), f["out"].view(np.uint32))
+    big = np.random.default_rng(3).uniform(-1, 1, (5000, 37)).astype(np.float32)
+    out = np.empty(5000, np.float32)
+    assert fe.fe_reduce_two_columns(ptr(big), 5000, 37, ptr(out)) == 0
+    assert np.array_equal(out.view(np.uint32), O.reduce_two_columns_dot(big).view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["dm_rotate_rows_p2", "dm_rotate_rows_m3", "dm_rotate_rows_p11", "dm_rotate_rows_p12",
+                                  "dm_rotate_cols_p3", "dm_rotate_cols_m5", "dm_rotate_cols_m30", "dm_rotate_cols_p13"])
+def test_rotate_golden(fe, name):
+    f = np.load(os.path.join(GOLDEN, name + ".npz"))
+    x = np.ascontiguousarray(f["in0"])
+    rows, cols, a = (int(v) for v in f["ints"])
+    out = np.empty_like(x)
+    assert fe.fe_rotate(ptr(x), rows, cols, a, 0 if "rows" in name else 1, ptr(out)) == 0
+    assert np.array_equal(out, f["out"].reshape(x.shape))
+
+
+def test_set_column_golden(fe):
+    f = np.load(os.path.join(GOLDEN, "dm_set_column.npz"))
+    x, v = np.ascontiguousarray(f["in0"]), np.ascontiguousarray(f["in1"])
+    rows, cols, col = (int(k) for k in f["ints"])
+    out = np.empty_like(x)
+    assert fe.fe_set_column(ptr(x), ptr(v), rows, cols, col, ptr(out)) == 0
+    assert np.array_equal(out, f["out"].reshape(x.shape))
+
+
+def _wrap(a):
+    return (np.asarray(a, np.int64) & 0xFFFFFFFF).astype(np.uint32).view(np.int32)
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (7, 5), (64, 64), (33, 1000), (1000, 3)], ids=lambda s: f"{s[0]}x{s[1]}")
+def test_dm_da_broadcast_zips(fe, shape):
+    rows, cols = shape
+    g = np.random.default_rng(rows * 3 + cols)
+    a = g.integers(-1000, 1000, shape, dtype=np.int32)
+    b = g.integers(-1000, 1000, shape, dtype=np.int32)
+    u, v, w = (g.integers(-1000, 1000, rows, dtype=np.int32) for _ in range(3))
+    r = np.arange(rows, dtype=np.int64)[:, None]
+    c = np.arange(cols, dtype=np.int64)[None, :]
+    A, B = a.astype(np.int64), b.astype(np.int64)
+    U, V, Wv = (z.astype(np.int64)[:, None] for z in (u, v, w))
+    want = {
+        0: 1000 * r + 7 * c + 2 * A - 3 * B + 5 * U,
+        1: 1000 * r + 7 * c - A + 11 * U,
+        2: 1000 * r + 7 * c + A - 2 * U + 3 * V - 5 * Wv,
+    }
+    out = np.empty(shape, np.int32)
+    for kind, exp in want.items():
+        assert fe.fe_dm_da(kind, ptr(a), ptr(b), ptr(u), ptr(v), ptr(w), rows, cols, ptr(out)) == 0
+        assert np.array_equal(out, _wrap(exp)), kind
+    if rows == cols:  # crossZipIndexInPlace: a[r][c] = b[c][r] + a[r][c]
+        assert fe.fe_dm_da(3, ptr(a), ptr(b), ptr(u), ptr(v), ptr(w), rows, cols, ptr(out)) == 0
+        assert np.array_equal(out, _wrap(B.T + A))
+    out1 = np.empty(rows, np.int32)
+    assert fe.fe_dm_da(4, ptr(a), ptr(b), ptr(u), ptr(v), ptr(w), rows, cols, ptr(out1)) == 0
+    i = np.arange(rows, dtype=np.int64)
+    assert np.array_equal(out1, _wrap(i + A.sum(axis=1) - u))
+    assert fe.fe_dm_da(5, ptr(a), ptr(b), ptr(u), ptr(v), ptr(w), rows, cols, ptr(out1)) == 0
+    assert np.array_equal(out1, _wrap(A[i, i % cols] * v + u + i))

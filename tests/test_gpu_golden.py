@@ -65,6 +65,24 @@ def run_on_gpu(A, name, f):
         return A.stencil3d_iterate(A.MSL_ST3_HEAT7, dx, out, 1, 0.0, ints[3], residual=False)[0].download()
     elif name.startswith("dc_boxsum"):
         return A.stencil3d_iterate(A.MSL_ST3_BOXSUM, dx, out, ints[3], 0.0, ints[4], residual=False)[0].download()
+    elif name.startswith("dm_reduce_rows_sum_i32"):
+        return A.fold_rows(A.MSL_FOLD_SUM, dx).download()
+    elif name == "dm_reduce_rows_max_f32":
+        return A.fold_rows(A.MSL_FOLD_MAX, dx).download()
+    elif name == "dm_reduce_two_columns":
+        pytest.skip("user-functor skeleton: checked through the C++ front end")
+    elif name.startswith("dm_rotate_rows"):
+        if abs(ints[2]) > ints[0]:  # the reference refuses and leaves the matrix as it is
+            with pytest.raises(A.MslError) as e:
+                A.rotate_rows(dx, out, ints[2])
+            assert e.value.code == A.MSL_ERR_NOT_IMPLEMENTED
+            return dx.download()
+        A.rotate_rows(dx, out, ints[2])
+    elif name.startswith("dm_rotate_cols"):
+        A.rotate_cols(dx, out, ints[2])
+    elif name == "dm_set_column":
+        A.set_column(dx, dy, ints[2])
+        return dx.download()
     else:
         raise KeyError(name)
     return tgt.download()
@@ -73,7 +91,9 @@ def run_on_gpu(A, name, f):
 @pytest.mark.parametrize("tma", [True, False], ids=["tma", "plain-loads"])
 @pytest.mark.parametrize("name", CASES)
 def test_gpu_matches_reference_golden(gpu, name, tma):
-    if not tma and not (name.startswith("dm_") or name.startswith("dc_")):
+    stencil = (name.startswith("dm_") or name.startswith("dc_")) and "index" not in name and not any(
+        name.startswith(p) for p in ("dm_reduce", "dm_rotate", "dm_set_column"))
+    if not tma and not stencil:
         pytest.skip("loader switch only affects stencils")
     f = np.load(os.path.join(GOLDEN, name + ".npz"))
     gpu.set_tma(tma)

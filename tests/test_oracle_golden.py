@@ -74,6 +74,22 @@ def oracle_for(name, f):
         return O.stencil3d_iterate(ST3_HEAT7, x, 1, 0.0, ints[3])[0]
     if name.startswith("dc_boxsum"):
         return O.stencil3d_iterate(ST3_BOXSUM, x, ints[3], 0.0, ints[4])[0]
+    if name.startswith("dm_reduce_rows_sum_i32"):
+        return O.fold_rows(MSL_FOLD_SUM, x)
+    if name == "dm_reduce_rows_max_f32":
+        return O.fold_rows(MSL_FOLD_MAX, x)
+    if name == "dm_reduce_two_columns":
+        return O.reduce_two_columns_dot(x)
+    if name.startswith("dm_rotate_rows"):
+        if abs(ints[2]) > ints[0]:  # the reference refuses and leaves the matrix as it is
+            with pytest.raises(RuntimeError):
+                O.rotate_rows(x, ints[2])
+            return x
+        return O.rotate_rows(x, ints[2])
+    if name.startswith("dm_rotate_cols"):
+        return O.rotate_cols(x, ints[2])
+    if name == "dm_set_column":
+        return O.set_column(x, y, ints[2])
     raise KeyError(name)
 
 
