@@ -312,6 +312,18 @@ int msl_server_release(void *server, long long request);
 int msl_server_stats(void *server, long long *completed, long long *active, long long *queued, size_t *device_bytes,
                      long long *intervals);
 /* Serve what was submitted, then stop the worker and free the device state. */
+/* Write every request the server holds to a file -- queued ones with their
+ * initial values, running ones with their latest iterate and sweep count
+ * (taken between two check intervals), finished ones with their result --
+ * together with the server's settings. halt != 0 stops the worker after the
+ * write: requests not finished stay unfinished (msl_server_wait reports it)
+ * and msl_server_stop then frees the server. */
+int msl_server_checkpoint(void *server, const char *path, int halt);
+/* Start a server from a checkpoint file: finished requests keep their
+ * results, running ones resume from their sweep count ahead of the queued
+ * ones, all under their original ids. Each result equals the one the
+ * uninterrupted server would have returned. */
+int msl_server_restore(const char *path, void **server);
 int msl_server_stop(void *server);
 
 /* ---- autotuner -------------------------------------------------------------

@@ -89,7 +89,8 @@ def load() -> ctypes.CDLL:
         "msl_server_release": [vp, ctypes.c_longlong],
         "msl_server_stats": [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                              ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(sz), ctypes.POINTER(ctypes.c_longlong)],
-        "msl_server_stop": [vp],
+        "msl_server_stop": [vp], "msl_server_checkpoint": [vp, ctypes.c_char_p, i],
+        "msl_server_restore": [ctypes.c_char_p, ctypes.POINTER(vp)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -289,6 +290,37 @@ class Server:
                                       ctypes.byref(i)), "msl_server_stats")
         return {"completed": c.value, "active": a.value, "queued": q.value, "device_bytes": b.value,
                 "intervals": i.value}
+
+    def checkpoint(self, path: str, halt: bool = False) -> None:
+        check(load().msl_server_checkpoint(self.handle, os.fsencode(path), 1 if halt else 0), "msl_server_checkpoint")
+
+    @staticmethod
+    def read_checkpoint_records(path: str):
+        """(id, kind, state, depth, rows, cols, sweeps, residual) of every request in a checkpoint file."""
+        with open(path, "rb") as f:
+            head = f.read(56)
+            count = int(np.frombuffer(head[48:56], np.int64)[0])
+            raw = f.read(48 * count)
+        out = []
+        for k in range(count):
+            rec = raw[48 * k:48 * (k + 1)]
+            rid = int(np.frombuffer(rec[:8], np.int64)[0])
+            kind, state, depth, rows, cols, _ = (int(v) for v in np.frombuffer(rec[8:32], np.int32))
+            it = int(np.frombuffer(rec[32:40], np.int64)[0])
+            res = float(np.frombuffer(rec[40:48], np.float64)[0])
+            out.append((rid, kind, state, depth, rows, cols, it, res))
+        return out
+
+    @classmethod
+    def restore(cls, path: str) -> "Server":
+        h = ctypes.c_void_p()
+        check(load().msl_server_restore(os.fsencode(path), ctypes.byref(h)), "msl_server_restore")
+        srv = cls.__new__(cls)
+        srv.handle = h
+        srv.shapes = {}
+        for rid, kind, _, depth, rows, cols, _, _ in cls.read_checkpoint_records(path):
+            srv.shapes[rid] = (rows, cols) if kind == MSL_SERVE_JACOBI2D else (depth, rows, cols)  # noqa: F821
+        return srv
 
     def stop(self) -> None:
         if self.handle:

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -86,7 +87,33 @@ struct Server {
     std::vector<int> map2, map3;
     std::vector<BatchGrid> h2;
     std::vector<ServeCube> h3;
+    // checkpoint request: written by the worker between intervals
+    std::string ckpt_path;
+    bool ckpt_pending = false, ckpt_halt = false, halted = false;
+    int ckpt_rc = MSL_OK;
+    std::string ckpt_error;
+    std::condition_variable cv_ckpt;
 };
+
+// Checkpoint file: "MSLSRV01", a CkptHeader, `count` CkptRecords, then per
+// record the request's values as FP32 (depth*rows*cols): the initial values
+// of a queued request, the latest iterate of a running one, the result of a
+// finished one. Host byte order.
+constexpr char kServerMagic[8] = {'M', 'S', 'L', 'S', 'R', 'V', '0', '1'};
+struct CkptHeader {
+    double tol;
+    int64_t max_iters;
+    int32_t check_every, depth2d;
+    uint64_t budget;
+    int64_t next_id, count;
+};
+struct CkptRecord {
+    int64_t id;
+    int32_t kind, state, depth, rows, cols, pad;
+    int64_t iters;
+    double residual;
+};
+static_assert(sizeof(CkptHeader) == 48 && sizeof(CkptRecord) == 48, "checkpoint layout");
 
 size_t iterate_bytes(const Request &r) { return 2 * ((r.cells() * sizeof(float) + 255) / 256 * 256); }
 
@@ -220,6 +247,53 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
     return cudaSuccess;
 }
 
+// Called by the worker with the lock held and no device work in flight.
+int write_checkpoint(Server &s, const std::string &path, std::string &why) {
+    std::vector<Request *> reqs;
+    for (Request *r : s.active) reqs.push_back(r);
+    for (Request *r : s.queue) reqs.push_back(r);
+    for (auto &kv : s.all)
+        if (kv.second->state == kDone) reqs.push_back(kv.second.get());
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) {
+        why = "cannot open " + path;
+        return MSL_ERR_INVALID_ARGUMENT;
+    }
+    CkptHeader h{s.tol, s.max_iters, s.check_every, s.depth2d, (uint64_t)s.budget, s.next_id, (int64_t)reqs.size()};
+    bool ok = fwrite(kServerMagic, 1, 8, f) == 8 && fwrite(&h, sizeof h, 1, f) == 1;
+    for (size_t i = 0; ok && i < reqs.size(); i++) {
+        const Request *r = reqs[i];
+        CkptRecord rec{r->id, r->kind, r->state, r->depth, r->rows, r->cols, 0, r->iters, r->residual};
+        ok = fwrite(&rec, sizeof rec, 1, f) == 1;
+    }
+    std::vector<float> h_buf;
+    for (size_t i = 0; ok && i < reqs.size(); i++) {
+        Request *r = reqs[i];
+        const float *src;
+        if (r->state == kRunning) {
+            h_buf.resize(r->cells());
+            cudaError_t e = cudaMemcpyAsync(h_buf.data(), r->buf[r->cur], r->cells() * sizeof(float),
+                                            cudaMemcpyDeviceToHost, s.s2);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s.s2);
+            if (e != cudaSuccess) {
+                fclose(f);
+                why = std::string("checkpoint copy: ") + cudaGetErrorString(e);
+                return MSL_ERR_CUDA;
+            }
+            src = h_buf.data();
+        } else {
+            src = r->state == kQueued ? r->init.data() : r->out.data();
+        }
+        ok = fwrite(src, sizeof(float), r->cells(), f) == r->cells();
+    }
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) {
+        why = "write to " + path + " failed";
+        return MSL_ERR_INVALID_ARGUMENT;
+    }
+    return MSL_OK;
+}
+
 void worker_loop(Server *sp) {
     Server &s = *sp;
     cudaSetDevice(s.device);
@@ -227,6 +301,16 @@ void worker_loop(Server *sp) {
         std::vector<Request *> act;
         {
             std::unique_lock<std::mutex> g(s.mu);
+            if (s.ckpt_pending) {  // no work in flight here: every active request sits at an interval end
+                s.ckpt_rc = write_checkpoint(s, s.ckpt_path, s.ckpt_error);
+                s.ckpt_pending = false;
+                s.halted = s.ckpt_halt && s.ckpt_rc == MSL_OK;
+                s.cv_ckpt.notify_all();
+                if (s.halted) {
+                    s.cv_done.notify_all();
+                    return;
+                }
+            }
             // admit in arrival order while memory and slots allow
             int n2 = 0, n3 = 0;
             for (Request *r : s.active) (r->kind == MSL_SERVE_JACOBI2D ? n2 : n3)++;
@@ -245,7 +329,7 @@ void worker_loop(Server *sp) {
             }
             if (s.active.empty()) {
                 if (s.stop) return;
-                s.cv_work.wait(g, [&] { return s.stop || !s.queue.empty(); });
+                s.cv_work.wait(g, [&] { return s.stop || !s.queue.empty() || s.ckpt_pending; });
                 continue;
             }
             act = s.active;
@@ -260,8 +344,7 @@ void worker_loop(Server *sp) {
             if (e == cudaSuccess) {
                 r->buf[0] = p;
                 r->buf[1] = (char *)p + half;
-                r->cur = 0;
-                r->iters = 0;
+                r->cur = 0;  // r->iters is 0, or the sweeps of a request resumed from a checkpoint
                 e = cudaMemcpyAsync(r->buf[0], r->init.data(), r->cells() * sizeof(float), cudaMemcpyHostToDevice, s.s2);
             }
             if (e != cudaSuccess) {
@@ -385,7 +468,7 @@ int msl_server_submit(void *server, int kind, int depth, int rows, int cols, con
         return rt::fail(MSL_ERR_BUDGET, "msl_server_submit: request needs %zu bytes, budget %zu", r->bytes, s->budget);
     std::lock_guard<std::mutex> g(s->mu);
     if (!s->error.empty()) return rt::fail(MSL_ERR_CUDA, "msl_server_submit: server failed: %s", s->error.c_str());
-    if (s->stop) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_submit: server is stopping");
+    if (s->stop || s->halted) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_submit: server is stopping");
     r->id = s->next_id++;
     r->t_submit = Clock::now();
     *request = r->id;
@@ -402,11 +485,13 @@ int msl_server_wait(void *server, long long request, double timeout_s) {
     auto it = s->all.find(request);
     if (it == s->all.end()) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_wait: unknown request %lld", request);
     Request *r = it->second.get();
-    auto pred = [&] { return r->state == kDone || r->state == kFailed; };
+    auto pred = [&] { return r->state == kDone || r->state == kFailed || s->halted; };
     if (timeout_s < 0) s->cv_done.wait(g, pred);
     else if (!s->cv_done.wait_for(g, std::chrono::duration<double>(timeout_s), pred))
         return rt::fail(MSL_ERR_TIMEOUT, "msl_server_wait: request %lld not finished", request);
     if (r->state == kFailed) return rt::fail(MSL_ERR_CUDA, "msl_server_wait: %s", s->error.c_str());
+    if (r->state != kDone)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_wait: the server halted after a checkpoint");
     return MSL_OK;
 }
 
@@ -448,6 +533,94 @@ int msl_server_stats(void *server, long long *completed, long long *active, long
     if (queued) *queued = (long long)s->queue.size();
     if (device_bytes) *device_bytes = s->used;
     if (intervals) *intervals = s->intervals;
+    return MSL_OK;
+}
+
+int msl_server_checkpoint(void *server, const char *path, int halt) {
+    Server *s = as_server(server);
+    if (!s || !path) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_checkpoint: NULL argument");
+    std::unique_lock<std::mutex> g(s->mu);
+    if (!s->error.empty()) return rt::fail(MSL_ERR_CUDA, "msl_server_checkpoint: server failed: %s", s->error.c_str());
+    if (s->halted || s->stop || s->ckpt_pending)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_checkpoint: server is stopping or busy");
+    s->ckpt_path = path;
+    s->ckpt_halt = halt != 0;
+    s->ckpt_pending = true;
+    s->cv_work.notify_all();
+    // the worker takes it between two intervals (one interval at most)
+    s->cv_ckpt.wait(g, [&] { return !s->ckpt_pending || !s->error.empty(); });
+    if (s->ckpt_pending) return rt::fail(MSL_ERR_CUDA, "msl_server_checkpoint: server failed: %s", s->error.c_str());
+    if (s->ckpt_rc != MSL_OK) return rt::fail(s->ckpt_rc, "msl_server_checkpoint: %s", s->ckpt_error.c_str());
+    return MSL_OK;
+}
+
+int msl_server_restore(const char *path, void **server) {
+    if (!path || !server) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_restore: NULL argument");
+    *server = nullptr;
+    FILE *f = fopen(path, "rb");
+    if (!f) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_restore: cannot open %s", path);
+    char magic[8];
+    CkptHeader h{};
+    bool ok = fread(magic, 1, 8, f) == 8 && !memcmp(magic, kServerMagic, 8) && fread(&h, sizeof h, 1, f) == 1 &&
+              h.count >= 0 && h.count <= (1 << 24) && h.check_every >= 1 && h.max_iters >= 1 &&
+              h.max_iters % h.check_every == 0;
+    std::vector<CkptRecord> recs;
+    if (ok) {
+        recs.resize((size_t)h.count);
+        ok = fread(recs.data(), sizeof(CkptRecord), recs.size(), f) == recs.size();
+    }
+    std::vector<std::unique_ptr<Request>> reqs;
+    for (size_t i = 0; ok && i < recs.size(); i++) {
+        const CkptRecord &c = recs[i];
+        ok = (c.kind == MSL_SERVE_JACOBI2D || c.kind == MSL_SERVE_HEAT3D) &&
+             (c.state == kQueued || c.state == kRunning || c.state == kDone) && c.depth >= 1 && c.rows >= 1 &&
+             c.cols >= 1 && (long long)c.depth * c.rows * c.cols <= (1LL << 31) - 1 && c.iters >= 0 &&
+             c.iters % h.check_every == 0 && c.id > 0 && c.id < h.next_id;
+        if (!ok) break;
+        auto r = std::make_unique<Request>();
+        r->id = c.id;
+        r->kind = c.kind;
+        r->depth = c.depth;
+        r->rows = c.rows;
+        r->cols = c.cols;
+        r->iters = c.iters;
+        r->residual = c.residual;
+        r->state = c.state;
+        std::vector<float> &dst = c.state == kDone ? r->out : r->init;
+        dst.resize(r->cells());
+        ok = fread(dst.data(), sizeof(float), dst.size(), f) == dst.size();
+        r->bytes = iterate_bytes(*r);
+        reqs.push_back(std::move(r));
+    }
+    fclose(f);
+    if (!ok) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_restore: %s is not a complete server checkpoint", path);
+    void *handle = nullptr;
+    if (int e = msl_server_start((size_t)h.budget, h.tol, h.max_iters, h.check_every, h.depth2d, &handle)) return e;
+    Server *s = as_server(handle);
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        const auto now = Clock::now();
+        s->next_id = h.next_id;
+        // running requests first (they were admitted before the queued ones), then the queue, in file order
+        for (int pass = 0; pass < 2; pass++)
+            for (auto &r : reqs) {
+                if (!r || r->state == kDone || (pass == 0) != (r->state == kRunning)) continue;
+                r->state = kQueued;
+                r->t_submit = now;
+                s->queue.push_back(r.get());
+                const long long id = r->id;
+                s->all[id] = std::move(r);
+            }
+        for (auto &r : reqs) {
+            if (!r) continue;
+            r->t_submit = r->t_admit = r->t_done = now;
+            s->completed++;
+            const long long id = r->id;
+            s->all[id] = std::move(r);
+        }
+        s->cv_work.notify_one();
+    }
+    *server = s;
     return MSL_OK;
 }
 

@@ -9,7 +9,7 @@ from oracle import pyoracle as O
 
 pytestmark = pytest.mark.gpu
 
-SPECIAL = [0.0, -0.0, np.nan, np.inf, -np.inf, 1e-40, -3.5e38, 1e-5, 123456.7, 1234567.0, 0.1, 2.0 / 3.0]
+SPECIAL = [0.0, -0.0, np.nan, np.inf, -np.inf, 1e-40, -3.0e38, 1e-5, 123456.7, 1234567.0, 0.1, 2.0 / 3.0]
 
 
 def grid(shape, dtype, seed):
