@@ -807,6 +807,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=400, help="requests of the serve workload (configs: 10000)")
     ap.add_argument("--serve-plain-sample", type=int, default=40)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[0.25, 0.5, 1.0, 2.0])
+    ap.add_argument("--stencil3d-persistent", type=int, default=-1, choices=[-1, 0, 1],
+                    help="3-D stencil kernel: 1 persistent, 0 one CTA per block, -1 library default")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -827,6 +829,7 @@ def main():
 
     from muesli4_gb300 import abi as A
     A.init(dist.local_rank)
+    A.set_stencil3d_persistent(args.stencil3d_persistent)
     w = WORKLOADS[args.workload](A)
     w.setup()
     ev = Events(A)

@@ -223,6 +223,11 @@ int msl_grid_load_text(const char *path, int dtype, void *grid, int depth, int r
  * identical either way; the switch exists to test and compare the loaders.
  * No reference counterpart (the reference has no staging). */
 int msl_set_tma(int enabled);
+/* 3-D stencils of radius <= 3: 1 = a persistent kernel (two CTAs per SM,
+ * each loading its next block with TMA while it computes the current one),
+ * 0 = one CTA per 64 x 16 x 8 block, -1 = the library's default (one CTA per
+ * block). Results are identical either way. */
+int msl_set_stencil3d_persistent(int mode);
 /* Sweeps fused into one launch by msl_stencil2d_iterate (temporal blocking:
  * the CTA runs depth-1 sweeps on a shared-memory tile with a depth*r halo and
  * writes the last; results are identical to single sweeps). 0 (default) uses

@@ -61,6 +61,7 @@ def load() -> ctypes.CDLL:
         "msl_init": [i], "msl_terminate": [], "msl_sync": [], "msl_get_stream": [ctypes.POINTER(vp)],
         "msl_set_stream": [vp], "msl_device_info": [ip, ctypes.POINTER(sz), ctypes.POINTER(sz)],
         "msl_launch_count": [ctypes.POINTER(ctypes.c_ulonglong)], "msl_set_tma": [i],
+        "msl_set_stencil3d_persistent": [i],
         "msl_alloc": [ctypes.POINTER(vp), sz], "msl_free": [vp], "msl_upload": [vp, vp, sz],
         "msl_download": [vp, vp, sz], "msl_copy": [vp, vp, sz], "msl_fill": [i, vp, sz, d],
         "msl_map": [i, i, vp, vp, sz, dp], "msl_zip": [i, i, vp, vp, vp, sz], "msl_zip3": [i, i, vp, vp, vp, vp, sz],
@@ -134,6 +135,11 @@ def launch_count() -> int:
 
 def set_tma(enabled: bool) -> None:
     check(load().msl_set_tma(1 if enabled else 0))
+
+
+def set_stencil3d_persistent(mode: int) -> None:
+    """3-D stencil kernel: 1 persistent, 0 one CTA per block, -1 default."""
+    check(load().msl_set_stencil3d_persistent(int(mode)), "msl_set_stencil3d_persistent")
 
 
 def set_temporal_depth(depth: int) -> None:

@@ -21,6 +21,9 @@ struct Sweep {
     bool tma;
 };
 
+// 3-D kernel choice of msl_set_stencil3d_persistent (-1 = default).
+std::atomic<int> g_persistent3d{-1};
+
 template <typename S>
 cudaError_t sweep2d(int kind, const S *in, S *out, int rows, int cols, int r, double neutral_d, const Sweep &sw) {
     using T = typename Compute<S>::type;
@@ -66,11 +69,12 @@ cudaError_t sweep3d(int kind, const S *in, S *out, int depth, int rows, int cols
     using T = typename Compute<S>::type;
     auto &c = ctx();
     const T neutral = (T)neutral_d;
+    const int pers = g_persistent3d.load(std::memory_order_relaxed);
     if (kind == MSL_ST3_HEAT7)
         return launch_stencil3d<S>(in, out, depth, rows, cols, r, neutral, StHeat7<T>{}, sw.resid, c.err_word, c.stream,
-                                   c.sm_count, sw.tma);
+                                   c.sm_count, sw.tma, pers);
     return launch_stencil3d<S>(in, out, depth, rows, cols, r, neutral, StBox3<T>{r, kind == MSL_ST3_BOXMEAN}, sw.resid,
-                               c.err_word, c.stream, c.sm_count, sw.tma);
+                               c.err_word, c.stream, c.sm_count, sw.tma, pers);
 }
 
 bool kind2_ok(int dtype, int kind) {
@@ -182,6 +186,12 @@ extern "C" {
 
 int msl_set_tma(int enabled) {
     g_tma_enabled.store(enabled ? 1 : 0);
+    return MSL_OK;
+}
+
+int msl_set_stencil3d_persistent(int mode) {
+    if (mode < -1 || mode > 1) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_set_stencil3d_persistent: %d not in -1..1", mode);
+    g_persistent3d.store(mode);
     return MSL_OK;
 }
 

@@ -87,28 +87,52 @@ template <typename T> struct StBoxAny {
 };
 // Conway's rule (examples/gameoflife.cpp:22-42), dead cells outside.
 struct StLife {
-    template <class V> __device__ __forceinline__ int32_t operator()(const V &m, int x, int y) const {
-        int32_t sum = m(x, y - 1) + m(x - 1, y - 1) + m(x + 1, y - 1) + m(x, y + 1) + m(x - 1, y + 1) +
-                      m(x + 1, y + 1) + m(x - 1, y) + m(x + 1, y);
-        int32_t alive = m(x, y);
+    static constexpr bool kStrip2 = true;
+    __device__ __forceinline__ static int32_t rule(int32_t alive, int32_t sum) {
         int32_t next = 0;
         if (alive == 1 && (sum == 2 || sum == 3)) next = 1;
         if (alive == 0 && sum == 3) next = 1;
         return next;
     }
+    template <class V> __device__ __forceinline__ int32_t operator()(const V &m, int x, int y) const {
+        int32_t sum = m(x, y - 1) + m(x - 1, y - 1) + m(x + 1, y - 1) + m(x, y + 1) + m(x - 1, y + 1) +
+                      m(x + 1, y + 1) + m(x - 1, y) + m(x + 1, y);
+        return rule(m(x, y), sum);
+    }
+    // kSt2RPT cells of one column. int32 addition wraps, so it is associative
+    // and commutative: the eight neighbours are summed as three-cell row sums
+    // (shared by the cells above and below) plus the left and right cells,
+    // which gives the same sum as the reference's order for any inputs.
+    template <class V> __device__ __forceinline__ void strip(const V &m, int x, int y0, int32_t (&out)[kSt2RPT]) const {
+        uint32_t l[kSt2RPT + 2], c[kSt2RPT + 2], r[kSt2RPT + 2], h[kSt2RPT + 2];
+#pragma unroll
+        for (int k = 0; k < kSt2RPT + 2; k++) {
+            l[k] = (uint32_t)m(x - 1, y0 - 1 + k);
+            c[k] = (uint32_t)m(x, y0 - 1 + k);
+            r[k] = (uint32_t)m(x + 1, y0 - 1 + k);
+            h[k] = l[k] + c[k] + r[k];
+        }
+#pragma unroll
+        for (int j = 0; j < kSt2RPT; j++)
+            out[j] = rule((int32_t)c[j + 1], (int32_t)(h[j] + h[j + 2] + l[j + 1] + r[j + 1]));
+    }
 };
 // heat3D: ((((((0 + W) + E) + N) + S) + B) + F) / 6 (examples/heatdiffusion.cpp:55-65).
 template <typename T> struct StHeat7 {
-    template <class V> __device__ __forceinline__ T operator()(const V &c, int x, int y, int z) const {
+    static constexpr bool kStar7 = true;
+    __device__ __forceinline__ T star7(T w, T e, T n, T s, T b, T f) const {
         T v = T(0);
-        v = Arith<T>::add(v, c(x - 1, y, z));
-        v = Arith<T>::add(v, c(x + 1, y, z));
-        v = Arith<T>::add(v, c(x, y - 1, z));
-        v = Arith<T>::add(v, c(x, y + 1, z));
-        v = Arith<T>::add(v, c(x, y, z - 1));
-        v = Arith<T>::add(v, c(x, y, z + 1));
+        v = Arith<T>::add(v, w);
+        v = Arith<T>::add(v, e);
+        v = Arith<T>::add(v, n);
+        v = Arith<T>::add(v, s);
+        v = Arith<T>::add(v, b);
+        v = Arith<T>::add(v, f);
         if constexpr (std::is_same<T, float>::value) return div6_rn(v);  // == v / 6, correctly rounded
         else return div_rn<T>(v, T(6));
+    }
+    template <class V> __device__ __forceinline__ T operator()(const V &c, int x, int y, int z) const {
+        return star7(c(x - 1, y, z), c(x + 1, y, z), c(x, y - 1, z), c(x, y + 1, z), c(x, y, z - 1), c(x, y, z + 1));
     }
 };
 // 3-D box, dx outer, dy, dz inner (examples/meanblur2.cpp:46-57).

@@ -139,6 +139,16 @@ template <typename A, typename B, typename C, typename D> constexpr int vec_widt
     return vec_width3<A, B, C>() < vec_width1<D>() ? vec_width3<A, B, C>() : vec_width1<D>();
 }
 
+// True for +0 (all bits zero): the value TMA and the plain staging loads
+// write outside a grid.
+template <typename T> MSL_HD bool is_positive_zero(T v) {
+    unsigned char b[sizeof(T)];
+    memcpy(b, &v, sizeof(T));
+    for (size_t i = 0; i < sizeof(T); i++)
+        if (b[i]) return false;
+    return true;
+}
+
 inline bool aligned_to(const void *p, size_t bytes) { return ((uintptr_t)p % bytes) == 0; }
 
 // ---- shared memory / mbarrier / TMA (inline PTX, sm_90+ incl. sm_103a) ----------
@@ -221,12 +231,13 @@ namespace gpu {
 // GPU test suite. The method needs a normal quotient, so inputs below 2^-122
 // in magnitude take IEEE division; infinities and NaNs pass through q.
 MSL_DEV float div6_rn(float x) {
-    if (fabsf(x) < 1.88079096131566e-37f) return __fdiv_rn(x, 6.0f);  // 2^-122
+    const float ax = fabsf(x);
+    // tiny (< 2^-122), infinite and NaN inputs: IEEE division
+    if (!(ax >= 1.88079096131566e-37f && ax <= 3.40282346638528859812e38f)) return __fdiv_rn(x, 6.0f);
     const float zh = 0.16666667163372039794921875f;  // RN(1/6)
     const float q = __fmul_rn(x, zh);
     const float r = __fmaf_rn(-q, 6.0f, x);
-    const float q2 = __fmaf_rn(r, zh, q);
-    return isfinite(q) ? q2 : q;
+    return __fmaf_rn(r, zh, q);
 }
 
 }  // namespace gpu

@@ -37,6 +37,7 @@
 
 #include <cuda.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "msl_device.cuh"
@@ -303,8 +304,11 @@ __global__ void __launch_bounds__(kSt2Threads)
         const int W = kSt2BX + 2 * ext, H = kSt2BY + 2 * ext;
         const int gx0 = x0 - ext, gy0 = y0 - ext;
         const bool interior = gx0 - r >= 0 && gy0 - r >= 0 && gx0 + W + r <= cols && gy0 + H + r <= rows;
-        auto sweep = [&](const NPLMatrix<T, S> &v) {
-            for (int row = warp; row < H; row += nwarps) {
+        // Cells of rows [row0, H) of the region, one at a time; cells outside
+        // the grid are left alone (the next sweep's view gives them the
+        // neutral value without reading them).
+        auto sweep_cells = [&](const NPLMatrix<T, S> &v, int row0) {
+            for (int row = row0 + warp; row < H; row += nwarps) {
                 const int gy = gy0 + row;
                 if ((unsigned)gy >= (unsigned)rows) continue;
                 for (int col = lane; col < W; col += 32) {
@@ -315,10 +319,28 @@ __global__ void __launch_bounds__(kSt2Threads)
         };
         if (interior) {
             m.check_ = false;
-            sweep(m);
+            if constexpr (has_strip2<Fn>::value) {
+                // whole kSt2RPT-row strips through the functor's strip(), the
+                // remaining rows cell by cell
+                const int nstrips = H / kSt2RPT, ngroups = (W + 31) / 32;
+                for (int item = warp; item < nstrips * ngroups; item += nwarps) {
+                    const int sidx = item / ngroups, col = (item - sidx * ngroups) * 32 + lane;
+                    if (col < W) {
+                        T vals[kSt2RPT];
+                        const int gx = gx0 + col, gy = gy0 + sidx * kSt2RPT;
+                        fn.strip(m, gx, gy, vals);
+                        S *d = dst + (gy - wy0) * pitch + (gx - wx0);
+#pragma unroll
+                        for (int j = 0; j < kSt2RPT; j++) d[j * pitch] = narrow<S>(vals[j]);
+                    }
+                }
+                sweep_cells(m, nstrips * kSt2RPT);
+            } else {
+                sweep_cells(m, 0);
+            }
         } else {
             m.check_ = true;
-            sweep(m);
+            sweep_cells(m, 0);
         }
         __syncthreads();
         m.tile_ = dst;
@@ -501,6 +523,88 @@ __global__ void __launch_bounds__(kSt3Threads, 5)
 // thread computes a 4-row x 8-plane strip of one column, all values before any
 // store. Used for radius <= kT3MaxR; larger radii use the z-march kernel.
 constexpr int kT3BX = 64, kT3BY = 16, kT3BZ = 8, kT3RPT = 4, kT3Threads = 256, kT3MaxR = 3;
+constexpr size_t kT3PipeSmemMax = 112 * 1024;  // two CTAs per SM
+
+// Functors that are a 7-point star -- a function of the six face neighbours
+// only -- may declare `static constexpr bool kStar7 = true` and provide
+// star7(W, E, N, S, B, F) (x-1, x+1, y-1, y+1, z-1, z+1), returning exactly
+// what operator() returns. Interior blocks then run star7_block: each window
+// value is read from shared memory once into a register and reused by every
+// cell of the strip that needs it, with the index arithmetic hoisted.
+template <class Fn, class = void> struct IsStar7 : std::false_type {};
+template <class Fn> struct IsStar7<Fn, std::void_t<decltype(Fn::kStar7)>> : std::bool_constant<Fn::kStar7> {};
+
+// One kT3RPT-row x kT3BZ-plane strip of an interior block. `box` holds the
+// block with halo (pitch x th x tz); (xl, yl, zl) is the box position of the
+// strip's first cell.
+template <typename S, bool FULL, class Fn>
+MSL_DEV void star7_block(const Fn &fn, const S *box, int pitch, int plane, int xl, int yl, int zl, int x, int ys,
+                         int z0, int depth, int rows, int cols, S *out, bool want, double &dmax) {
+    using T = typename Compute<S>::type;
+    const S *p = box + zl * plane + yl * pitch + xl;
+    T cm[kT3RPT], c0[kT3RPT], cp[kT3RPT];
+#pragma unroll
+    for (int j = 0; j < kT3RPT; j++) {
+        cm[j] = widen<S>(p[j * pitch - plane]);
+        c0[j] = widen<S>(p[j * pitch]);
+    }
+    S *o = out + ((size_t)z0 * rows + ys) * cols + x;
+    const size_t oplane = (size_t)rows * cols;
+#pragma unroll
+    for (int k = 0; k < kT3BZ; k++) {
+        const S *q = p + k * plane;
+#pragma unroll
+        for (int j = 0; j < kT3RPT; j++) cp[j] = widen<S>(q[j * pitch + plane]);
+        const T n = widen<S>(q[-pitch]), sth = widen<S>(q[kT3RPT * pitch]);
+#pragma unroll
+        for (int j = 0; j < kT3RPT; j++) {
+            const T w = widen<S>(q[j * pitch - 1]), e = widen<S>(q[j * pitch + 1]);
+            const T v = fn.star7(w, e, j == 0 ? n : c0[j - 1], j == kT3RPT - 1 ? sth : c0[j + 1], cm[j], cp[j]);
+            const S sv = narrow<S>(v);
+            if (FULL || (x < cols && ys + j < rows && z0 + k < depth)) {
+                if (want) {
+                    const double d = fabs(stored_f64(sv) - (double)c0[j]);
+                    if (d > dmax || d != d) dmax = d;
+                }
+                o[(size_t)j * cols] = sv;
+            }
+        }
+        o += oplane;
+#pragma unroll
+        for (int j = 0; j < kT3RPT; j++) {
+            cm[j] = c0[j];
+            c0[j] = cp[j];
+        }
+    }
+}
+
+// Interior blocks of the persistent kernel: every value of the strip is
+// computed before the first store, so no store separates the shared-memory
+// reads of neighbouring planes and rows and the compiler can keep each window
+// value in a register for all the cells that read it.
+template <typename S, bool FULL, class Fn, class View>
+MSL_DEV void stencil3d_block_regs(const Fn &fn, const View &c, int x, int ys, int z0, int depth, int rows, int cols,
+                                  S *out, bool want, double &dmax) {
+    using T = typename Compute<S>::type;
+    T vals[kT3BZ][kT3RPT];
+#pragma unroll
+    for (int k = 0; k < kT3BZ; k++)
+#pragma unroll
+        for (int j = 0; j < kT3RPT; j++) vals[k][j] = fn(c, x, ys + j, z0 + k);
+#pragma unroll
+    for (int k = 0; k < kT3BZ; k++) {
+        S *o = out + ((size_t)(z0 + k) * rows + ys) * cols + x;
+#pragma unroll
+        for (int j = 0; j < kT3RPT; j++) {
+            if (!FULL && !(x < cols && ys + j < rows && z0 + k < depth)) continue;
+            if (want) {
+                const double d = fabs(stored_f64(narrow<S>(vals[k][j])) - (double)c(x, ys + j, z0 + k));
+                if (d > dmax || d != d) dmax = d;
+            }
+            o[(size_t)j * cols] = narrow<S>(vals[k][j]);
+        }
+    }
+}
 
 template <typename S, bool FULL, class Fn, class View>
 MSL_DEV void stencil3d_block(const Fn &fn, const View &c, int x, int ys, int z0, int depth, int rows, int cols, S *out,
@@ -589,13 +693,151 @@ __global__ void __launch_bounds__(kT3Threads, 3)
     const bool interior = wx0 >= 0 && wy0 >= 0 && wz0 >= 0 && wx0 + pitch <= cols && wy0 + th <= rows &&
                           wz0 + tz <= depth;
     const bool want = resid != nullptr;
+    // Outside the grid the staged box holds zeros (TMA fill, or the plain
+    // loads below): with a +0 neutral value the view needs no bounds test.
+    const bool zero_fill = is_positive_zero(neutral);
     double dmax = 0.0;
+    if constexpr (IsStar7<Fn>::value) {
+        if (interior || zero_fill) {
+            const int xl = x - wx0, yl = ys - wy0, zl = z0 - wz0;
+            if (interior)
+                star7_block<S, true>(fn, box, pitch, pitch * th, xl, yl, zl, x, ys, z0, depth, rows, cols, out, want,
+                                     dmax);
+            else
+                star7_block<S, false>(fn, box, pitch, pitch * th, xl, yl, zl, x, ys, z0, depth, rows, cols, out, want,
+                                      dmax);
+            if (want) {
+                dmax = block_max(dmax);
+                if (threadIdx.x == 0) atomic_max_nonneg(resid, dmax);
+            }
+            return;
+        }
+    }
     if (interior) {
         c.check_ = false;
         stencil3d_block<S, true>(fn, c, x, ys, z0, depth, rows, cols, out, want, dmax);
     } else {
-        c.check_ = true;
+        c.check_ = !zero_fill;
         stencil3d_block<S, false>(fn, c, x, ys, z0, depth, rows, cols, out, want, dmax);
+    }
+    if (want) {
+        dmax = block_max(dmax);
+        if (threadIdx.x == 0) atomic_max_nonneg(resid, dmax);
+    }
+}
+
+// Persistent, double-buffered form of the 3-D tile kernel (TMA only). Each
+// CTA walks the blocks blockIdx.x, blockIdx.x + gridDim.x, ... (x fastest,
+// then y, then z); the TMA load of its next block runs while it computes the
+// current one, so the load latency no longer serialises with the arithmetic.
+// Two CTAs per SM; results and residual are those of stencil3d_tile_kernel.
+template <typename S> MSL_HD size_t t3_box_bytes(int r, int hx) {
+    return ((size_t)(kT3BX + 2 * hx) * (kT3BY + 2 * r) * (kT3BZ + 2 * r) * sizeof(S) + 127) / 128 * 128;
+}
+
+template <typename S, class Fn>
+__global__ void __launch_bounds__(kT3Threads, 2)
+    stencil3d_pipe_kernel(const __grid_constant__ CUtensorMap tmap, const S *in, S *out, int depth, int rows,
+                          int cols, int r, int hx, typename Compute<S>::type neutral, Fn fn,
+                          unsigned long long *resid, unsigned *err) {
+    using T = typename Compute<S>::type;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);  // one mbarrier per buffer
+    const unsigned box_bytes = (unsigned)t3_box_bytes<S>(r, hx);
+    // buffer k at smem_raw + kStHeader + k * box_bytes (computed from smem_raw
+    // each time, so the compiler keeps shared-memory addressing)
+    auto buffer = [&](int k) { return reinterpret_cast<S *>(smem_raw + kStHeader + k * box_bytes); };
+    const int pitch = kT3BX + 2 * hx, th = kT3BY + 2 * r, tz = kT3BZ + 2 * r;
+    const uint32_t tx_bytes = (uint32_t)(pitch * th * tz * sizeof(S));
+    const unsigned nbx = (cols + kT3BX - 1) / kT3BX, nbxy = nbx * ((rows + kT3BY - 1) / kT3BY);
+    const unsigned nblocks = nbxy * ((depth + kT3BZ - 1) / kT3BZ);  // < 2^31 (checked by the launcher)
+    unsigned b = blockIdx.x;
+    if (b >= nblocks) return;
+    auto origin = [&](unsigned blk, int &x0, int &y0, int &z0) {
+        const unsigned bz = blk / nbxy, rem = blk - bz * nbxy, by = rem / nbx;
+        x0 = (int)(rem - by * nbx) * kT3BX;
+        y0 = (int)by * kT3BY;
+        z0 = (int)bz * kT3BZ;
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+        int x0, y0, z0;
+        origin(b, x0, y0, z0);
+        mbar_arrive_expect_tx(&bar[0], tx_bytes);
+        tma_load_3d(buffer(0), &tmap, &bar[0], x0 - hx, y0 - r, z0 - r);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool want = resid != nullptr;
+    const bool zero_fill = is_positive_zero(neutral);
+    double dmax = 0.0;
+    PLCube<T, S> c;
+    c.width = cols;
+    c.height = rows;
+    c.depth = depth;
+    c.stencilSize = r;
+    c.neutralValue = neutral;
+    c.global_ = in;
+    c.pitch_ = pitch;
+    c.tile_h_ = th;
+    c.plane_ = pitch * th;
+    c.mask_ = -1;
+    for (int i = 0; b < nblocks; b += gridDim.x, i++) {
+        const unsigned nb = b + gridDim.x;
+        if (threadIdx.x == 0 && nb < nblocks) {  // prefetch the next block into the other buffer
+            int x0, y0, z0;
+            origin(nb, x0, y0, z0);
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bar[(i + 1) & 1], tx_bytes);
+            tma_load_3d(buffer((i + 1) & 1), &tmap, &bar[(i + 1) & 1], x0 - hx, y0 - r, z0 - r);
+        }
+        bool ok = mbar_wait_bounded(&bar[i & 1], (uint32_t)(i >> 1) & 1u, err);
+        ok = __syncthreads_and(ok);
+        if (!ok) {  // let the prefetch land before the CTA gives up its shared memory
+            if (threadIdx.x == 0 && nb < nblocks) mbar_wait_bounded(&bar[(i + 1) & 1], (uint32_t)((i + 1) >> 1) & 1u, err);
+            __syncthreads();
+            return;
+        }
+        int x0, y0, z0;
+        origin(b, x0, y0, z0);
+        const int wx0 = x0 - hx, wy0 = y0 - r, wz0 = z0 - r;
+        S *box = buffer(i & 1);
+        c.ring_ = box;
+        c.ox_ = wx0;
+        c.oy_ = wy0;
+        c.oz_ = wz0;
+        c.zlo_ = wz0;
+        c.zhi_ = wz0 + tz - 1;
+        const int x = x0 + (warp % (kT3BX / 32)) * 32 + lane;
+        const int ys = y0 + (warp / (kT3BX / 32)) * kT3RPT;
+        const bool interior = wx0 >= 0 && wy0 >= 0 && wz0 >= 0 && wx0 + pitch <= cols && wy0 + th <= rows &&
+                              wz0 + tz <= depth;
+        if (interior || zero_fill) {
+            // The box holds the neutral value wherever it lies outside the
+            // grid (TMA fills those elements with zeros), so the view needs
+            // no bounds test; boundary blocks only mask their stores.
+            c.check_ = false;
+            const int xl = x - wx0, yl = ys - wy0, zl = z0 - wz0;
+            if constexpr (IsStar7<Fn>::value) {
+                if (interior)
+                    star7_block<S, true>(fn, box, pitch, pitch * th, xl, yl, zl, x, ys, z0, depth, rows, cols,
+                                         out, want, dmax);
+                else
+                    star7_block<S, false>(fn, box, pitch, pitch * th, xl, yl, zl, x, ys, z0, depth, rows, cols,
+                                          out, want, dmax);
+            } else {
+                if (interior)
+                    stencil3d_block_regs<S, true>(fn, c, x, ys, z0, depth, rows, cols, out, want, dmax);
+                else
+                    stencil3d_block_regs<S, false>(fn, c, x, ys, z0, depth, rows, cols, out, want, dmax);
+            }
+        } else {
+            c.check_ = true;
+            stencil3d_block<S, false>(fn, c, x, ys, z0, depth, rows, cols, out, want, dmax);
+        }
+        __syncthreads();  // every read of this buffer is done before it is loaded again
     }
     if (want) {
         dmax = block_max(dmax);
@@ -724,18 +966,26 @@ template <typename S> inline size_t stencil3d_tile_smem(int r) {
            (size_t)(kT3BX + 2 * halo_x<S>(r)) * (kT3BY + 2 * r) * (kT3BZ + 2 * r) * sizeof(S);
 }
 
+// persistent: 1 = the persistent double-buffered kernel where it applies,
+// 0 or -1 (the default) = one CTA per block. On GB300 the one-CTA-per-block
+// kernel runs four CTAs per SM and overlaps loads and arithmetic across them;
+// it measured faster than the two-CTA persistent kernel on heat3D 512^3.
 template <typename S, class Fn>
 cudaError_t launch_stencil3d_tile(const S *in, S *out, int depth, int rows, int cols, int r,
                                   typename Compute<S>::type neutral, Fn fn, unsigned long long *resid, unsigned *err,
-                                  cudaStream_t st, bool allow_tma) {
+                                  cudaStream_t st, bool allow_tma, int persistent = -1) {
     const int hx = halo_x<S>(r);
     const int pitch = kT3BX + 2 * hx, th = kT3BY + 2 * r, tz = kT3BZ + 2 * r;
     const size_t smem = stencil3d_tile_smem<S>(r);
     dim3 grid((cols + kT3BX - 1) / kT3BX, (rows + kT3BY - 1) / kT3BY, (depth + kT3BZ - 1) / kT3BZ);
     CUtensorMap map{};
     const bool tma = allow_tma && stencil_tma_ok<S>(in, cols, pitch, th) && tz <= 256;
+    // Double buffering when two CTAs of two boxes each fit an SM.
+    const size_t pipe_smem = (size_t)kStHeader + 2 * t3_box_bytes<S>(r, hx);
+    const bool pipe = persistent == 1 && sizeof(S) <= 4 && tma && pipe_smem <= kT3PipeSmemMax &&
+                      (long long)grid.x * grid.y * grid.z < (1LL << 31);
     auto k = tma ? stencil3d_tile_kernel<S, Fn, true> : stencil3d_tile_kernel<S, Fn, false>;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!pipe && smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (tma) {
         cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)depth};
         cuuint64_t strides[2] = {(cuuint64_t)cols * sizeof(S), (cuuint64_t)cols * rows * sizeof(S)};
@@ -746,6 +996,20 @@ cudaError_t launch_stencil3d_tile(const S *in, S *out, int depth, int rows, int 
                                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return cudaErrorInvalidValue;
     }
+    if constexpr (sizeof(S) <= 4) {
+        if (pipe) {
+            auto kp = stencil3d_pipe_kernel<S, Fn>;
+            cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pipe_smem);
+            const long long nblocks = (long long)grid.x * grid.y * grid.z;
+            int sms = 0, dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            const long long ctas = std::min<long long>(nblocks, 2LL * (sms > 0 ? sms : 152));
+            kp<<<(unsigned)ctas, kT3Threads, pipe_smem, st>>>(map, in, out, depth, rows, cols, r, hx, neutral, fn,
+                                                              resid, err);
+            return cudaGetLastError();
+        }
+    }
     k<<<grid, kT3Threads, smem, st>>>(map, in, out, depth, rows, cols, r, hx, neutral, fn, resid, err);
     return cudaGetLastError();
 }
@@ -753,9 +1017,10 @@ cudaError_t launch_stencil3d_tile(const S *in, S *out, int depth, int rows, int 
 template <typename S, class Fn>
 cudaError_t launch_stencil3d(const S *in, S *out, int depth, int rows, int cols, int r,
                              typename Compute<S>::type neutral, Fn fn, unsigned long long *resid, unsigned *err,
-                             cudaStream_t st, int sm_count, bool allow_tma = true) {
+                             cudaStream_t st, int sm_count, bool allow_tma = true, int persistent = -1) {
     if (r <= kT3MaxR && stencil3d_tile_smem<S>(r) <= 120 * 1024)
-        return launch_stencil3d_tile<S>(in, out, depth, rows, cols, r, neutral, fn, resid, err, st, allow_tma);
+        return launch_stencil3d_tile<S>(in, out, depth, rows, cols, r, neutral, fn, resid, err, st, allow_tma,
+                                        persistent);
     const int hx = halo_x<S>(r);
     const int pitch = kSt3BX + 2 * hx, th = kSt3BY + 2 * r;
     const int ns_log2 = st3_ns_log2(r);

@@ -317,26 +317,38 @@ def test_stencil_argument_errors(gpu):
 SHAPES_3D = [(1, 1, 1), (5, 7, 11), (12, 10, 14), (33, 17, 70), (40, 64, 64), (20, 33, 200)]
 
 
-@pytest.mark.parametrize("tma", [True, False], ids=["tma", "plain"])
+@pytest.mark.parametrize("kernel", ["tma", "plain", "persistent"])
 @pytest.mark.parametrize("shape", SHAPES_3D, ids=str)
-def test_stencil3d_heat(gpu, shape, tma):
+def test_stencil3d_heat(gpu, shape, kernel):
+    """heat3D (7-point register path) on the one-CTA-per-block kernel with TMA
+    or plain staging loads, and on the persistent double-buffered kernel; a
+    non-zero neutral value takes the bounds-tested view on boundary blocks."""
     x = W.heat_cube(*shape, seed=sum(shape))
-    gpu.set_tma(tma)
+    gpu.set_tma(kernel != "plain")
+    gpu.set_stencil3d_persistent(1 if kernel == "persistent" else 0)
     try:
-        a, b = dev(gpu, x), gpu.DeviceArray(x.shape, x.dtype)
-        last, res = gpu.stencil3d_iterate(gpu.MSL_ST3_HEAT7, a, b, 1, 0.0, 3)
-        want, _, want_res = O.stencil3d_iterate(gpu.MSL_ST3_HEAT7, x, 1, 0.0, 3)
-        assert bits_equal(last.download(), want)
-        assert res == want_res
+        for neutral in (0.0, 0.75):
+            a, b = dev(gpu, x), gpu.DeviceArray(x.shape, x.dtype)
+            last, res = gpu.stencil3d_iterate(gpu.MSL_ST3_HEAT7, a, b, 1, neutral, 3)
+            want, _, want_res = O.stencil3d_iterate(gpu.MSL_ST3_HEAT7, x, 1, neutral, 3)
+            assert bits_equal(last.download(), want), neutral
+            assert res == want_res
     finally:
         gpu.set_tma(True)
+        gpu.set_stencil3d_persistent(-1)
 
 
+@pytest.mark.parametrize("persistent", [0, 1])
 @pytest.mark.parametrize("r", [1, 2, 3])
 @pytest.mark.parametrize("shape", [(9, 10, 11), (24, 20, 68)], ids=str)
-def test_stencil3d_box(gpu, r, shape):
+def test_stencil3d_box(gpu, r, shape, persistent):
     x = W.heat_cube(*shape, seed=r)
     d, o = dev(gpu, x), gpu.DeviceArray(x.shape, x.dtype)
-    for kind in (gpu.MSL_ST3_BOXSUM, gpu.MSL_ST3_BOXMEAN):
-        gpu.stencil3d(kind, d, o, r, 0.5)
-        assert bits_equal(o.download(), O.stencil3d(kind, x, r, 0.5)), (kind, r)
+    gpu.set_stencil3d_persistent(persistent)
+    try:
+        for kind in (gpu.MSL_ST3_BOXSUM, gpu.MSL_ST3_BOXMEAN):
+            for neutral in (0.5, 0.0):
+                gpu.stencil3d(kind, d, o, r, neutral)
+                assert bits_equal(o.download(), O.stencil3d(kind, x, r, neutral)), (kind, r, neutral)
+    finally:
+        gpu.set_stencil3d_persistent(-1)
