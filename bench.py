@@ -807,6 +807,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=400, help="requests of the serve workload (configs: 10000)")
     ap.add_argument("--serve-plain-sample", type=int, default=40)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[0.25, 0.5, 1.0, 2.0])
+    ap.add_argument("--temporal-depth", type=int, default=0,
+                    help="sweeps per launch of the iterated 2-D stencils (0: the autotuner's choice)")
     ap.add_argument("--stencil3d-persistent", type=int, default=-1, choices=[-1, 0, 1],
                     help="3-D stencil kernel: 1 persistent, 0 one CTA per block, -1 library default")
     args = ap.parse_args()
@@ -832,6 +834,13 @@ def main():
     A.set_stencil3d_persistent(args.stencil3d_persistent)
     w = WORKLOADS[args.workload](A)
     w.setup()
+    if args.temporal_depth > 0:  # after setup: overrides the autotuner's record
+        A.set_temporal_depth(args.temporal_depth)
+        if hasattr(w, "tuned") and "life_temporal_depth" in w.tuned:
+            w.tuned["life_temporal_depth"] = args.temporal_depth
+            p = w.parts["life"]
+            p.launches = (w.life_steps + args.temporal_depth - 1) // args.temporal_depth
+            p.bytes_per_launch = 8 * w.side ** 2 * w.life_steps // p.launches
     ev = Events(A)
     for _ in range(args.warmup):
         w.step()

@@ -3,6 +3,7 @@
 // (element type, functor, radius, grid-size class). The reference fixes its
 // tiling statically (tile width 16, include/muesli.h:195; 1024-thread blocks,
 // src/muesli.cpp:103).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <map>
@@ -36,6 +37,28 @@ int tuned_depth(int dtype, int kind, int rows, int cols, int radius) {
     return it == table().end() ? 1 : it->second.depth;
 }
 
+// Fill a tuning grid with a pseudo-random 0/1 pattern (a valid input for
+// every built-in functor; a constant grid would hide data-dependent branches).
+// `one` is the element bit pattern of 1 in the grid's element type.
+__global__ void tune_fill_kernel(unsigned char *p, size_t n, int es, unsigned long long one) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        unsigned h = (unsigned)i * 2654435761u;
+        h ^= h >> 15;
+        const unsigned long long v = ((h >> 7) % 10u) < 3u ? one : 0ull;  // about 30 % ones
+        for (int k = 0; k < es; k++) p[i * es + k] = (unsigned char)(v >> (8 * k));
+    }
+}
+
+unsigned long long one_bits(int dtype) {
+    switch (dtype) {
+        case MSL_F32: return 0x3F800000ull;
+        case MSL_F64: return 0x3FF0000000000000ull;
+        case MSL_I32: return 1ull;
+        default: return 0x3F80ull;  // MSL_BF16
+    }
+}
+
 }  // namespace rt
 }  // namespace msl
 
@@ -59,8 +82,8 @@ int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, 
         cudaFree(a);
         return rt::fail(MSL_ERR_OUT_OF_MEMORY, "msl_autotune_stencil2d: scratch grids");
     }
-    // A 0/1 pattern is a valid input for every built-in functor and element type.
-    cudaMemsetAsync(a, 0, bytes, c.stream);
+    rt::tune_fill_kernel<<<(unsigned)(c.sm_count * 8), 256, 0, c.stream>>>((unsigned char *)a, (size_t)rows * cols,
+                                                                            (int)es, rt::one_bits(dtype));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -69,30 +92,43 @@ int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, 
     int rc = MSL_OK;
     const int saved = 0;
     const int candidates[] = {1, 2, 3, 4, 6, 8};
-    for (int d : candidates) {
-        if (d > iters) break;
-        if (msl_set_temporal_depth(d) != MSL_OK) continue;
-        int inb = 0;
-        // warm-up, then timed
-        rc = msl_stencil2d_iterate(dtype, kind, a, b, rows, cols, radius, 0.0, d, nullptr, &inb);
-        if (rc != MSL_OK) {
-            if (d == 1) break;  // the functor itself is not available: report it
-            rc = MSL_OK;        // this depth does not fit: skip it
-            continue;
-        }
-        cudaEventRecord(e0, c.stream);
-        rc = msl_stencil2d_iterate(dtype, kind, a, b, rows, cols, radius, 0.0, iters, nullptr, &inb);
-        cudaEventRecord(e1, c.stream);
-        if (rc != MSL_OK) break;
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        const double rate = (double)rows * cols * iters / (ms * 1e-3);
-        if (rate > best_r) {
-            best_r = rate;
-            best = d;
+    const int ncand = (int)(sizeof candidates / sizeof candidates[0]);
+    double rate[ncand] = {};
+    bool usable[ncand] = {};
+    // Warm every depth up once, then time each three times, interleaved, and
+    // keep each depth's best run (clock ramps and other work on the GPU slow
+    // single runs down, never speed them up).
+    for (int round = 0; round < 4 && rc == MSL_OK; round++) {
+        for (int k = 0; k < ncand; k++) {
+            const int d = candidates[k];
+            if (d > iters || (round > 0 && !usable[k])) continue;
+            if (msl_set_temporal_depth(d) != MSL_OK) continue;
+            int inb = 0;
+            if (round == 0) {
+                rc = msl_stencil2d_iterate(dtype, kind, a, b, rows, cols, radius, 0.0, d, nullptr, &inb);
+                if (rc != MSL_OK) {
+                    if (d == 1) break;  // the functor itself is not available: report it
+                    rc = MSL_OK;        // this depth does not fit: skip it
+                    continue;
+                }
+                usable[k] = true;
+                continue;
+            }
+            cudaEventRecord(e0, c.stream);
+            rc = msl_stencil2d_iterate(dtype, kind, a, b, rows, cols, radius, 0.0, iters, nullptr, &inb);
+            cudaEventRecord(e1, c.stream);
+            if (rc != MSL_OK) break;
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            rate[k] = std::max(rate[k], (double)rows * cols * iters / (ms * 1e-3));
         }
     }
+    for (int k = 0; k < ncand; k++)
+        if (usable[k] && rate[k] > best_r) {
+            best_r = rate[k];
+            best = candidates[k];
+        }
     msl_set_temporal_depth(saved);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -304,11 +304,11 @@ __global__ void __launch_bounds__(kSt2Threads)
         const int W = kSt2BX + 2 * ext, H = kSt2BY + 2 * ext;
         const int gx0 = x0 - ext, gy0 = y0 - ext;
         const bool interior = gx0 - r >= 0 && gy0 - r >= 0 && gx0 + W + r <= cols && gy0 + H + r <= rows;
-        // Cells of rows [row0, H) of the region, one at a time; cells outside
-        // the grid are left alone (the next sweep's view gives them the
-        // neutral value without reading them).
-        auto sweep_cells = [&](const NPLMatrix<T, S> &v, int row0) {
-            for (int row = row0 + warp; row < H; row += nwarps) {
+        // Every cell of the region, one at a time; cells outside the grid are
+        // left alone (the next sweep's view gives them the neutral value
+        // without reading them).
+        auto sweep_cells = [&](const NPLMatrix<T, S> &v) {
+            for (int row = warp; row < H; row += nwarps) {
                 const int gy = gy0 + row;
                 if ((unsigned)gy >= (unsigned)rows) continue;
                 for (int col = lane; col < W; col += 32) {
@@ -320,27 +320,43 @@ __global__ void __launch_bounds__(kSt2Threads)
         if (interior) {
             m.check_ = false;
             if constexpr (has_strip2<Fn>::value) {
-                // whole kSt2RPT-row strips through the functor's strip(), the
-                // remaining rows cell by cell
-                const int nstrips = H / kSt2RPT, ngroups = (W + 31) / 32;
-                for (int item = warp; item < nstrips * ngroups; item += nwarps) {
-                    const int sidx = item / ngroups, col = (item - sidx * ngroups) * 32 + lane;
-                    if (col < W) {
-                        T vals[kSt2RPT];
-                        const int gx = gx0 + col, gy = gy0 + sidx * kSt2RPT;
-                        fn.strip(m, gx, gy, vals);
-                        S *d = dst + (gy - wy0) * pitch + (gx - wx0);
+                // The block's own 64 columns in whole kSt2RPT-row strips
+                // through the functor's strip() (two full warps per strip
+                // row)...
+                const int nstrips = H / kSt2RPT, sr = nstrips * kSt2RPT;
+                for (int item = warp; item < 2 * nstrips; item += nwarps) {
+                    const int sidx = item >> 1, col = ext + (item & 1) * 32 + lane;
+                    T vals[kSt2RPT];
+                    const int gx = gx0 + col, gy = gy0 + sidx * kSt2RPT;
+                    fn.strip(m, gx, gy, vals);
+                    S *d = dst + (gy - wy0) * pitch + (gx - wx0);
 #pragma unroll
-                        for (int j = 0; j < kSt2RPT; j++) d[j * pitch] = narrow<S>(vals[j]);
-                    }
+                    for (int j = 0; j < kSt2RPT; j++) d[j * pitch] = narrow<S>(vals[j]);
                 }
-                sweep_cells(m, nstrips * kSt2RPT);
+                // ...then the margin cells spread over all threads: the two
+                // ext-wide side columns (rows 0..H-1), then the rows below the
+                // strips.
+                const int side = ext * H, total = 2 * side + (H - sr) * kSt2BX;
+                for (int t = threadIdx.x; t < total; t += blockDim.x) {
+                    int row, col;
+                    if (t < 2 * side) {
+                        const int u = t < side ? t : t - side, rr = u / ext;
+                        row = rr;
+                        col = (t < side ? 0 : ext + kSt2BX) + (u - rr * ext);
+                    } else {
+                        const int u = t - 2 * side;
+                        row = sr + u / kSt2BX;
+                        col = ext + u % kSt2BX;
+                    }
+                    const int gx = gx0 + col, gy = gy0 + row;
+                    dst[(gy - wy0) * pitch + (gx - wx0)] = narrow<S>(fn(m, gx, gy));
+                }
             } else {
-                sweep_cells(m, 0);
+                sweep_cells(m);
             }
         } else {
             m.check_ = true;
-            sweep_cells(m, 0);
+            sweep_cells(m);
         }
         __syncthreads();
         m.tile_ = dst;
