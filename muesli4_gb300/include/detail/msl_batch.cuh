@@ -38,6 +38,10 @@ struct BatchGrid {
 // The plain-Jacobi functor: boundary cells keep their value, inside cells
 // take (((0 + W) + E) + N) + S times 0.25 (heatdiffusion order; x*0.25 == x/4).
 struct JacobiFn {
+    static constexpr bool kStrip2 = true;
+    template <class V, typename T> __device__ __forceinline__ void strip(const V &m, int x, int y0, T (&out)[kSt2RPT]) const {
+        heat5_strip<true>(m, x, y0, out);
+    }
     template <class V> __device__ __forceinline__ auto operator()(const V &m, int x, int y) const -> decltype(m(x, y)) {
         using T = decltype(m(x, y));
         if (x == 0 || y == 0 || x == m.width - 1 || y == m.height - 1) return m(x, y);
@@ -140,7 +144,7 @@ __global__ void __launch_bounds__(kSt2Threads)
     const int buf_elems = (pitch * th * (int)sizeof(S) + 127) / 128 * 128 / (int)sizeof(S);
     S *buf0 = reinterpret_cast<S *>(smem_raw + kStHeader);
     S *buf1 = buf0 + buf_elems;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     JacobiFn fn;
     for (long long item = blockIdx.x; item < total_tiles; item += gridDim.x) {
         BatchGrid &g = grids[list[tile_grid[item]]];  // tile_grid: work-list position of the tile's grid
@@ -170,32 +174,7 @@ __global__ void __launch_bounds__(kSt2Threads)
         m.oy_ = wy0;
         m.pitch_ = pitch;
         m.tile_h_ = th;
-        S *dst = buf1;
-        for (int s = 1; s < depth; s++) {
-            const int ext = (depth - s) * r;
-            const int W = kSt2BX + 2 * ext, H = kSt2BY + 2 * ext;
-            const int gx0 = x0 - ext, gy0 = y0 - ext;
-            auto sweep = [&](const NPLMatrix<T, S> &v) {
-                for (int row = warp; row < H; row += nwarps) {
-                    const int gy = gy0 + row;
-                    if ((unsigned)gy >= (unsigned)rows) continue;
-                    for (int col = lane; col < W; col += 32) {
-                        const int gx = gx0 + col;
-                        if ((unsigned)gx < (unsigned)cols) dst[(gy - wy0) * pitch + (gx - wx0)] = narrow<S>(fn(v, gx, gy));
-                    }
-                }
-            };
-            if (gx0 - r >= 0 && gy0 - r >= 0 && gx0 + W + r <= cols && gy0 + H + r <= rows) {
-                m.check_ = false;
-                sweep(m);
-            } else {
-                m.check_ = true;
-                sweep(m);
-            }
-            __syncthreads();
-            m.tile_ = dst;
-            dst = (dst == buf1) ? buf0 : buf1;
-        }
+        tb_inner_sweeps<S>(fn, m, buf0, buf1, x0, y0, rows, cols, r, depth, pitch, wx0, wy0);
         const int x = x0 + (warp % (kSt2BX / 32)) * 32 + lane;
         const int ys = y0 + (warp / (kSt2BX / 32)) * kSt2RPT;
         double dmax = 0.0;

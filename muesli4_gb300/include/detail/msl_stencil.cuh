@@ -112,6 +112,34 @@ template <typename S> MSL_HD int halo_x(int r) {
     return (r + q - 1) / q * q;
 }
 
+// heat2D of one cell from its four neighbours: (((0 + W) + E) + N) + S, then
+// times 0.25 (== / 4 for every value: both round the same real number once).
+template <typename T> MSL_DEV T heat5_value(T w, T e, T n, T s) {
+    T v = T(0);
+    v = Arith<T>::add(v, w);
+    v = Arith<T>::add(v, e);
+    v = Arith<T>::add(v, n);
+    v = Arith<T>::add(v, s);
+    return Arith<T>::mul(v, T(0.25));
+}
+
+// kSt2RPT cells of column x from row y0 of the 5-point heat2D stencil
+// (JACOBI: boundary cells of the grid keep their value): the column's
+// kSt2RPT + 2 values are read once and serve as N, S and centre of the cells.
+template <bool JACOBI, class V, typename T>
+MSL_DEV void heat5_strip(const V &m, int x, int y0, T (&out)[kSt2RPT]) {
+    T c[kSt2RPT + 2];
+#pragma unroll
+    for (int k = 0; k < kSt2RPT + 2; k++) c[k] = m(x, y0 - 1 + k);
+    const bool xb = JACOBI && (x == 0 || x == m.width - 1);
+#pragma unroll
+    for (int j = 0; j < kSt2RPT; j++) {
+        const int y = y0 + j;
+        if (JACOBI && (xb || y == 0 || y == m.height - 1)) out[j] = c[j + 1];
+        else out[j] = heat5_value<T>(m(x - 1, y), m(x + 1, y), c[j], c[j + 2]);
+    }
+}
+
 // Functors may provide strip(view, x, y0, vals) computing kSt2RPT vertically
 // adjacent cells at once (register reuse); others are called per cell.
 template <class F, class = void> struct has_strip2 : std::false_type {};
@@ -174,6 +202,82 @@ MSL_DEV void stencil2d_strip(const Fn &fn, const View &m, int x, int ys, int row
 #pragma unroll
     for (int j = 0; j < kSt2RPT; j++)
         if (FULL || ys + j < rows) o[(size_t)j * cols] = narrow<S>(vals[j]);
+}
+
+// Sweeps 1 .. depth-1 of a temporally blocked 64 x 32 tile whose window
+// (pitch wide, origin (wx0, wy0)) is staged in buf0: sweep s computes the
+// block grown by (depth - s) * r on every side into the other buffer, so the
+// last sweep (left to the caller) has all the cells it reads. On return
+// m.tile_ points at the buffer holding sweep depth-1 (buf0 when depth == 1).
+template <typename S, class Fn>
+MSL_DEV void tb_inner_sweeps(const Fn &fn, NPLMatrix<typename Compute<S>::type, S> &m, S *buf0, S *buf1, int x0,
+                             int y0, int rows, int cols, int r, int depth, int pitch, int wx0, int wy0) {
+    using T = typename Compute<S>::type;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    S *dst = buf1;
+    for (int s = 1; s < depth; s++) {
+        const int ext = (depth - s) * r;  // halo the remaining sweeps still need
+        const int W = kSt2BX + 2 * ext, H = kSt2BY + 2 * ext;
+        const int gx0 = x0 - ext, gy0 = y0 - ext;
+        const bool interior = gx0 - r >= 0 && gy0 - r >= 0 && gx0 + W + r <= cols && gy0 + H + r <= rows;
+        // Every cell of the region, one at a time; cells outside the grid are
+        // left alone (the next sweep's view gives them the neutral value
+        // without reading them).
+        auto sweep_cells = [&](const NPLMatrix<T, S> &v) {
+            for (int row = warp; row < H; row += nwarps) {
+                const int gy = gy0 + row;
+                if ((unsigned)gy >= (unsigned)rows) continue;
+                for (int col = lane; col < W; col += 32) {
+                    const int gx = gx0 + col;
+                    if ((unsigned)gx < (unsigned)cols) dst[(gy - wy0) * pitch + (gx - wx0)] = narrow<S>(fn(v, gx, gy));
+                }
+            }
+        };
+        if (interior) {
+            m.check_ = false;
+            if constexpr (has_strip2<Fn>::value) {
+                // The block's own 64 columns in whole kSt2RPT-row strips
+                // through the functor's strip() (two full warps per strip
+                // row)...
+                const int nstrips = H / kSt2RPT, sr = nstrips * kSt2RPT;
+                for (int item = warp; item < 2 * nstrips; item += nwarps) {
+                    const int sidx = item >> 1, col = ext + (item & 1) * 32 + lane;
+                    T vals[kSt2RPT];
+                    const int gx = gx0 + col, gy = gy0 + sidx * kSt2RPT;
+                    fn.strip(m, gx, gy, vals);
+                    S *d = dst + (gy - wy0) * pitch + (gx - wx0);
+#pragma unroll
+                    for (int j = 0; j < kSt2RPT; j++) d[j * pitch] = narrow<S>(vals[j]);
+                }
+                // ...then the margin cells spread over all threads: the two
+                // ext-wide side columns (rows 0..H-1), then the rows below the
+                // strips.
+                const int side = ext * H, total = 2 * side + (H - sr) * kSt2BX;
+                for (int t = threadIdx.x; t < total; t += blockDim.x) {
+                    int row, col;
+                    if (t < 2 * side) {
+                        const int u = t < side ? t : t - side, rr = u / ext;
+                        row = rr;
+                        col = (t < side ? 0 : ext + kSt2BX) + (u - rr * ext);
+                    } else {
+                        const int u = t - 2 * side;
+                        row = sr + u / kSt2BX;
+                        col = ext + u % kSt2BX;
+                    }
+                    const int gx = gx0 + col, gy = gy0 + row;
+                    dst[(gy - wy0) * pitch + (gx - wx0)] = narrow<S>(fn(m, gx, gy));
+                }
+            } else {
+                sweep_cells(m);
+            }
+        } else {
+            m.check_ = true;
+            sweep_cells(m);
+        }
+        __syncthreads();
+        m.tile_ = dst;
+        dst = (dst == buf1) ? buf0 : buf1;
+    }
 }
 
 // One CTA = one 64 x 32 output block. Dynamic smem: [0,128) mbarrier, then the
@@ -297,71 +401,8 @@ __global__ void __launch_bounds__(kSt2Threads)
     m.oy_ = wy0;
     m.pitch_ = pitch;
     m.tile_h_ = th;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    S *dst = buf1;
-    for (int s = 1; s < depth; s++) {
-        const int ext = (depth - s) * r;  // halo the remaining sweeps still need
-        const int W = kSt2BX + 2 * ext, H = kSt2BY + 2 * ext;
-        const int gx0 = x0 - ext, gy0 = y0 - ext;
-        const bool interior = gx0 - r >= 0 && gy0 - r >= 0 && gx0 + W + r <= cols && gy0 + H + r <= rows;
-        // Every cell of the region, one at a time; cells outside the grid are
-        // left alone (the next sweep's view gives them the neutral value
-        // without reading them).
-        auto sweep_cells = [&](const NPLMatrix<T, S> &v) {
-            for (int row = warp; row < H; row += nwarps) {
-                const int gy = gy0 + row;
-                if ((unsigned)gy >= (unsigned)rows) continue;
-                for (int col = lane; col < W; col += 32) {
-                    const int gx = gx0 + col;
-                    if ((unsigned)gx < (unsigned)cols) dst[(gy - wy0) * pitch + (gx - wx0)] = narrow<S>(fn(v, gx, gy));
-                }
-            }
-        };
-        if (interior) {
-            m.check_ = false;
-            if constexpr (has_strip2<Fn>::value) {
-                // The block's own 64 columns in whole kSt2RPT-row strips
-                // through the functor's strip() (two full warps per strip
-                // row)...
-                const int nstrips = H / kSt2RPT, sr = nstrips * kSt2RPT;
-                for (int item = warp; item < 2 * nstrips; item += nwarps) {
-                    const int sidx = item >> 1, col = ext + (item & 1) * 32 + lane;
-                    T vals[kSt2RPT];
-                    const int gx = gx0 + col, gy = gy0 + sidx * kSt2RPT;
-                    fn.strip(m, gx, gy, vals);
-                    S *d = dst + (gy - wy0) * pitch + (gx - wx0);
-#pragma unroll
-                    for (int j = 0; j < kSt2RPT; j++) d[j * pitch] = narrow<S>(vals[j]);
-                }
-                // ...then the margin cells spread over all threads: the two
-                // ext-wide side columns (rows 0..H-1), then the rows below the
-                // strips.
-                const int side = ext * H, total = 2 * side + (H - sr) * kSt2BX;
-                for (int t = threadIdx.x; t < total; t += blockDim.x) {
-                    int row, col;
-                    if (t < 2 * side) {
-                        const int u = t < side ? t : t - side, rr = u / ext;
-                        row = rr;
-                        col = (t < side ? 0 : ext + kSt2BX) + (u - rr * ext);
-                    } else {
-                        const int u = t - 2 * side;
-                        row = sr + u / kSt2BX;
-                        col = ext + u % kSt2BX;
-                    }
-                    const int gx = gx0 + col, gy = gy0 + row;
-                    dst[(gy - wy0) * pitch + (gx - wx0)] = narrow<S>(fn(m, gx, gy));
-                }
-            } else {
-                sweep_cells(m);
-            }
-        } else {
-            m.check_ = true;
-            sweep_cells(m);
-        }
-        __syncthreads();
-        m.tile_ = dst;
-        dst = (dst == buf1) ? buf0 : buf1;
-    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    tb_inner_sweeps<S>(fn, m, buf0, buf1, x0, y0, rows, cols, r, depth, pitch, wx0, wy0);
     const int x = x0 + (warp % (kSt2BX / 32)) * 32 + lane;
     const int ys = y0 + (warp / (kSt2BX / 32)) * kSt2RPT;
     const bool interior = x0 - r >= 0 && y0 - r >= 0 && x0 + kSt2BX + r <= cols && y0 + kSt2BY + r <= rows;
