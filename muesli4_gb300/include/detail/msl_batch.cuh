@@ -157,11 +157,7 @@ __global__ void __launch_bounds__(kSt2Threads)
         S *out = (S *)g.buf[g.cur ^ 1];
         const int wx0 = x0 - hx, wy0 = y0 - depth * r;
         __syncthreads();  // previous item's readers are done with the buffers
-        for (int i = threadIdx.x; i < pitch * th; i += blockDim.x) {
-            const int ty = i / pitch, tx = i - ty * pitch;
-            const int gx = wx0 + tx, gy = wy0 + ty;
-            buf0[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows) ? in[(size_t)gy * cols + gx] : S{};
-        }
+        stage_window<S>(buf0, in, pitch, th, th, wx0, wy0, 0, 1, rows, cols);
         __syncthreads();
         NPLMatrix<T, S> m;
         m.width = cols;

@@ -23,15 +23,19 @@ struct ServeCube {
 
 // heat3D (examples/heatdiffusion.cpp:55-65), Dirichlet 0 outside the cube.
 struct Heat7Fn {
-    template <class V> __device__ __forceinline__ float operator()(const V &c, int x, int y, int z) const {
+    static constexpr bool kStar7 = true;
+    __device__ __forceinline__ float star7(float w, float e, float n, float s, float b, float f) const {
         float v = 0.0f;
-        v = __fadd_rn(v, c(x - 1, y, z));
-        v = __fadd_rn(v, c(x + 1, y, z));
-        v = __fadd_rn(v, c(x, y - 1, z));
-        v = __fadd_rn(v, c(x, y + 1, z));
-        v = __fadd_rn(v, c(x, y, z - 1));
-        v = __fadd_rn(v, c(x, y, z + 1));
+        v = __fadd_rn(v, w);
+        v = __fadd_rn(v, e);
+        v = __fadd_rn(v, n);
+        v = __fadd_rn(v, s);
+        v = __fadd_rn(v, b);
+        v = __fadd_rn(v, f);
         return div6_rn(v);
+    }
+    template <class V> __device__ __forceinline__ float operator()(const V &c, int x, int y, int z) const {
+        return star7(c(x - 1, y, z), c(x + 1, y, z), c(x, y - 1, z), c(x, y + 1, z), c(x, y, z - 1), c(x, y, z + 1));
     }
 };
 
@@ -54,36 +58,21 @@ static __global__ void __launch_bounds__(kT3Threads, 3)
         float *out = (float *)cb.buf[cb.cur ^ 1];
         const int wx0 = x0 - hx, wy0 = y0 - r, wz0 = z0 - r;
         __syncthreads();  // the previous item's readers are done with the box
-        for (int i = threadIdx.x; i < pitch * th * tz; i += blockDim.x) {
-            const int zz = i / (pitch * th), rem = i - zz * pitch * th, yy = rem / pitch, xx = rem - yy * pitch;
-            const int gx = wx0 + xx, gy = wy0 + yy, gz = wz0 + zz;
-            box[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows && gz >= 0 && gz < depth)
-                         ? in[((size_t)gz * rows + gy) * cols + gx]
-                         : 0.0f;
-        }
+        stage_window<float>(box, in, pitch, th, th * tz, wx0, wy0, wz0, depth, rows, cols);
         __syncthreads();
-        PLCube<float> c;
-        c.width = cols;
-        c.height = rows;
-        c.depth = depth;
-        c.stencilSize = r;
-        c.neutralValue = 0.0f;
-        c.ring_ = box;
-        c.global_ = in;
-        c.ox_ = wx0;
-        c.oy_ = wy0;
-        c.oz_ = wz0;
-        c.pitch_ = pitch;
-        c.tile_h_ = th;
-        c.plane_ = pitch * th;
-        c.mask_ = -1;
-        c.zlo_ = wz0;
-        c.zhi_ = wz0 + tz - 1;
-        c.check_ = true;
+        // The staged box holds zeros outside the cube (Dirichlet 0), so every
+        // block runs the 7-point register path; boundary blocks mask stores.
         const int x = x0 + (warp % (kT3BX / 32)) * 32 + lane;
         const int ys = y0 + (warp / (kT3BX / 32)) * kT3RPT;
+        const bool interior = wx0 >= 0 && wy0 >= 0 && wz0 >= 0 && wx0 + pitch <= cols && wy0 + th <= rows &&
+                              wz0 + tz <= depth;
         double dmax = 0.0;
-        stencil3d_block<float, false>(fn, c, x, ys, z0, depth, rows, cols, out, check != 0, dmax);
+        if (interior)
+            star7_block<float, true>(fn, box, pitch, pitch * th, x - wx0, ys - wy0, z0 - wz0, x, ys, z0, depth, rows,
+                                     cols, out, check != 0, dmax);
+        else
+            star7_block<float, false>(fn, box, pitch, pitch * th, x - wx0, ys - wy0, z0 - wz0, x, ys, z0, depth, rows,
+                                      cols, out, check != 0, dmax);
         if (check) {
             dmax = block_max(dmax);
             if (threadIdx.x == 0) atomic_max_nonneg(&cb.resid_bits, dmax);

@@ -112,6 +112,26 @@ template <typename S> MSL_HD int halo_x(int r) {
     return (r + q - 1) / q * q;
 }
 
+// Stage a window of `nrows` rows (pitch elements each) with plain coalesced
+// loads: window row k is grid row (wy0 + k % th) of plane (wz0 + k / th); the
+// elements outside the grid become zero. One warp per window row, so the row
+// and plane come from one division per row rather than per element.
+template <typename S>
+MSL_DEV void stage_window(S *dst, const S *in, int pitch, int th, int nrows, int wx0, int wy0, int wz0, int depth,
+                          int rows, int cols) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int k = warp; k < nrows; k += nwarps) {
+        const int zz = k / th, gy = wy0 + (k - zz * th), gz = wz0 + zz;
+        const bool row_in = gy >= 0 && gy < rows && gz >= 0 && gz < depth;
+        const S *src = in + ((size_t)(row_in ? gz : 0) * rows + (row_in ? gy : 0)) * cols;
+        S *d = dst + (size_t)k * pitch;
+        for (int xx = lane; xx < pitch; xx += 32) {
+            const int gx = wx0 + xx;
+            d[xx] = (row_in && gx >= 0 && gx < cols) ? src[gx] : S{};
+        }
+    }
+}
+
 // heat2D of one cell from its four neighbours: (((0 + W) + E) + N) + S, then
 // times 0.25 (== / 4 for every value: both round the same real number once).
 template <typename T> MSL_DEV T heat5_value(T w, T e, T n, T s) {
@@ -307,11 +327,7 @@ __global__ void __launch_bounds__(kSt2Threads)
         }
         ok = mbar_wait_bounded(bar, 0, err);
     } else {
-        for (int i = threadIdx.x; i < pitch * th; i += blockDim.x) {
-            const int ty = i / pitch, tx = i - ty * pitch;
-            const int gx = wx0 + tx, gy = wy0 + ty;
-            tile[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows) ? in[(size_t)gy * cols + gx] : S{};
-        }
+        stage_window<S>(tile, in, pitch, th, th, wx0, wy0, 0, 1, rows, cols);
     }
     ok = __syncthreads_and(ok);
     if (!ok) return;
@@ -381,11 +397,7 @@ __global__ void __launch_bounds__(kSt2Threads)
         }
         ok = mbar_wait_bounded(bar, 0, err);
     } else {
-        for (int i = threadIdx.x; i < pitch * th; i += blockDim.x) {
-            const int ty = i / pitch, tx = i - ty * pitch;
-            const int gx = wx0 + tx, gy = wy0 + ty;
-            buf0[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows) ? in[(size_t)gy * cols + gx] : S{};
-        }
+        stage_window<S>(buf0, in, pitch, th, th, wx0, wy0, 0, 1, rows, cols);
     }
     ok = __syncthreads_and(ok);
     if (!ok) return;
@@ -499,13 +511,7 @@ __global__ void __launch_bounds__(kSt3Threads, 5)
                 mbar_arrive_expect_tx(&bars[p & mask], plane_bytes);
                 tma_load_3d(dst, &tmap, &bars[p & mask], wx0, wy0, p);
             } else {
-                for (int i = threadIdx.x; i < pitch * th; i += blockDim.x) {
-                    const int ty = i / pitch, tx = i - ty * pitch;
-                    const int gx = wx0 + tx, gy = wy0 + ty;
-                    dst[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows && p >= 0 && p < depth)
-                                 ? in[((size_t)p * rows + gy) * cols + gx]
-                                 : S{};
-                }
+                stage_window<S>(dst, in, pitch, th, th, wx0, wy0, p, depth, rows, cols);
             }
         };
         auto wait = [&](int p) {
@@ -716,13 +722,7 @@ __global__ void __launch_bounds__(kT3Threads, 3)
         }
         ok = mbar_wait_bounded(bar, 0, err);
     } else {
-        for (int i = threadIdx.x; i < pitch * th * tz; i += blockDim.x) {
-            const int zz = i / (pitch * th), rem = i - zz * pitch * th, yy = rem / pitch, xx = rem - yy * pitch;
-            const int gx = wx0 + xx, gy = wy0 + yy, gz = wz0 + zz;
-            box[i] = (gx >= 0 && gx < cols && gy >= 0 && gy < rows && gz >= 0 && gz < depth)
-                         ? in[((size_t)gz * rows + gy) * cols + gx]
-                         : S{};
-        }
+        stage_window<S>(box, in, pitch, th, th * tz, wx0, wy0, wz0, depth, rows, cols);
     }
     ok = __syncthreads_and(ok);
     if (!ok) return;
