@@ -160,9 +160,9 @@ int msl_fold(int dtype, int op, const void *in, size_t n, void *result);
 int msl_fold_absdiff_max(int dtype, const void *a, const void *b, size_t n, double *result);
 
 /* Fold that allocates nothing, for callers that cannot allocate device memory
- * (code enqueuing work during a CUDA-graph stream capture, loops that must
- * never pay cudaMalloc's implicit synchronisation, hosts whose device memory
- * belongs to another allocator). It needs no msl_init: it runs on the current
+ * (loops that must never pay cudaMalloc's implicit synchronisation, plugins
+ * running inside a host whose device memory belongs to that host's own
+ * allocator). It needs no msl_init: it runs on the current
  * device and `stream` (a cudaStream_t; NULL is the default stream) and writes
  * one element of dtype to the device pointer result_device; the caller
  * synchronises. Its scratch is a static device array of 2048 CTA partials

@@ -1,10 +1,9 @@
 // msl_fold_noalloc: the fold skeleton for callers that must not allocate.
 //
-// Some callers cannot call cudaMalloc: code that enqueues work while a stream
-// is being captured into a CUDA graph (allocation calls are not permitted in
-// that state), real-time loops that must never hit the implicit device
-// synchronisation cudaMalloc/cudaFree can cause, and hosts whose device memory
-// is entirely owned by another allocator. msl_fold needs msl_init, which
+// Some callers cannot call cudaMalloc: real-time loops that must never hit the
+// implicit device synchronisation cudaMalloc/cudaFree can cause, and plugins
+// running inside a host whose device memory is entirely owned by that host's
+// own allocator. msl_fold needs msl_init, which
 // allocates the fold scratch; this variant needs nothing but the caller's
 // input, the caller's one-element device result and a stream.
 //

@@ -1,9 +1,8 @@
 """msl_fold_noalloc: the fold entry point that allocates nothing.
 
-It serves callers that cannot allocate device memory -- work enqueued while a
-stream is captured into a CUDA graph, loops that must not pay the implicit
-synchronisation of cudaMalloc/cudaFree, hosts whose device memory belongs to
-another allocator. Its scratch is a static device array, so its results are
+It serves callers that cannot allocate device memory -- loops that must not
+pay the implicit synchronisation of cudaMalloc/cudaFree, plugins inside a host
+whose device memory belongs to that host's own allocator. Its scratch is a static device array, so its results are
 checked against the allocating msl_fold on the same input, twice in a row
 (the second call reuses the array the first one left behind). The test itself
 allocates the input and the one-element result; the entry point does not.
