@@ -794,6 +794,13 @@ def run_batch(args, dist: Dist):
         print(json.dumps(line), flush=True)
 
 
+DRAM_TRAFFIC_PER_LAUNCH = {
+    "heat3d": 1027.49e6,         # profiles/heat7_stencil3d_512.md (one sweep of 512^3)
+    "life": 495.25e6,            # profiles/life8_stencil2d_8192.md (two sweeps of 8192^2)
+    "box_mean_r1-10": 500.23e6,  # profiles/boxmean_r10_stencil2d_8192.md (r = 10)
+}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -903,11 +910,11 @@ def main():
                               "GB_per_s": pp.bytes_per_launch * pp.launches / t / 1e9 if t > 0 else None}
         if w.unit == "GCUPS":
             parts_out[pp.name]["GCUPS"] = pp.updates / t / 1e9 if t > 0 else None
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as f:
-            traffic = json.load(f).get(f"{w.name}:{p.name}")
+    # DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum +
+    # dram__bytes_write.sum) from the ncu captures summarised in profiles/.
+    traffic = DRAM_TRAFFIC_PER_LAUNCH.get(p.name)
+    if p.name == "life" and getattr(w, "tuned", {}).get("life_temporal_depth") != 2:
+        traffic = None  # captured at temporal depth 2
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
