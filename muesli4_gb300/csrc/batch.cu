@@ -120,7 +120,7 @@ int solve_t(Batch &b, double tol, long long max_iters, int check_every, int dept
         MSL_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b.resident_smem),
                      "msl_batch_solve");
         k<<<(unsigned)b.resident.size(), kBatchResidentThreads, b.resident_smem, b.side>>>(b.dev, b.d_lists, tol, max_iters,
-                                                                                           check_every);
+                                                                                           check_every, max_iters);
         MSL_TRY_CUDA(cudaGetLastError(), "msl_batch_solve: resident kernel");
         rt::count_launch();
         MSL_TRY_CUDA(cudaEventRecord(b.join, b.side), "msl_batch_solve");
@@ -145,7 +145,8 @@ int solve_t(Batch &b, double tol, long long max_iters, int check_every, int dept
         MSL_TRY_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "msl_batch_solve: capture");
         for (int j = 0; j < rounds; j++) {
             const int check = ((j + 1) % chunk_rounds) == 0;
-            rk<<<(unsigned)grid, kSt2Threads, smem, st>>>(b.dev, wl, b.d_tile_grid, b.total_tiles, depth, check);
+            rk<<<(unsigned)grid, kSt2Threads, smem, st>>>(b.dev, wl, b.d_tile_grid, b.total_tiles, depth, check,
+                                                           nullptr, 0, 0.0, 0, nullptr);
             batch_finalize_kernel<<<1, 256, 0, st>>>(b.dev, wl, nlist, depth, check, tol, max_iters, b.d_active);
         }
         cudaError_t ce = cudaStreamEndCapture(st, &graph);

@@ -21,6 +21,7 @@
 // No reference counterpart: the reference solves one container at a time.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
@@ -42,6 +43,7 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 constexpr int kMaxActive = 4096;  // active requests of each kind
+constexpr size_t kResidentSmem = 200 * 1024;  // both iterates of a shared-memory-resident 2-D request
 
 enum ReqState { kQueued = 0, kRunning = 1, kDone = 2, kFailed = 3 };
 
@@ -56,6 +58,7 @@ struct Request {
     int cur = 0;
     long long iters = 0;
     double residual = 0.0;
+    int waited = 0;          // consecutive intervals this running request was not scheduled
     int state = kQueued;     // read and written under the server lock
     bool finished = false;   // set by the worker when the request converged or ran out of sweeps
     size_t cells() const { return (size_t)depth * rows * cols; }
@@ -76,8 +79,9 @@ struct Server {
     std::deque<Request *> queue;
     std::vector<Request *> active;
     std::map<long long, std::unique_ptr<Request>> all;
-    cudaStream_t s2 = nullptr, s3 = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t s2 = nullptr, s3 = nullptr, sr = nullptr;  // 2-D rounds, 3-D rounds, resident 2-D grids
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_res_fork = nullptr, ev_res_join = nullptr;
+    unsigned *d_ticket = nullptr;  // last-CTA tickets of the 2-D and 3-D round kernels
     BatchGrid *d2 = nullptr;
     ServeCube *d3 = nullptr;
     int *dlist = nullptr;  // 0..kMaxActive-1
@@ -151,17 +155,28 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
     s.h3.clear();
     s.map2.clear();
     s.map3.clear();
-    std::vector<Request *> r2, r3;
+    std::vector<Request *> r2, r3, res2;
     long long tiles = 0, blocks = 0;
+    size_t res_smem = 0;
+    auto grid2d = [](const Request *r) {
+        BatchGrid g{};
+        g.buf[0] = r->buf[0];
+        g.buf[1] = r->buf[1];
+        g.rows = r->rows;
+        g.cols = r->cols;
+        g.cur = r->cur;
+        g.iters = r->iters;
+        return g;
+    };
     for (Request *r : act) {
         if (r->kind == MSL_SERVE_JACOBI2D) {
-            BatchGrid g{};
-            g.buf[0] = r->buf[0];
-            g.buf[1] = r->buf[1];
-            g.rows = r->rows;
-            g.cols = r->cols;
-            g.cur = r->cur;
-            g.iters = r->iters;
+            const size_t need = 2 * ((r->cells() * sizeof(float) + 127) / 128 * 128);
+            if (need <= kResidentSmem) {  // whole grid in shared memory: one launch per interval
+                res2.push_back(r);
+                res_smem = std::max(res_smem, need);
+                continue;
+            }
+            BatchGrid g = grid2d(r);
             g.first_tile = tiles;
             const long long nt = (long long)((r->cols + kSt2BX - 1) / kSt2BX) * ((r->rows + kSt2BY - 1) / kSt2BY);
             tiles += nt;
@@ -186,28 +201,48 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
             r3.push_back(r);
         }
     }
-    const int n2 = (int)s.h2.size(), n3 = (int)s.h3.size();
+    const int nw = (int)s.h2.size();  // work-list grids first, then the resident ones
+    for (Request *r : res2) {
+        s.h2.push_back(grid2d(r));
+        r2.push_back(r);
+    }
+    const int n2 = (int)s.h2.size(), n3 = (int)s.h3.size(), nres = n2 - nw;
     SERVE_TRY(cudaEventRecord(s.ev_fork, s.s2));
     SERVE_TRY(cudaStreamWaitEvent(s.s3, s.ev_fork, 0));
     if (n2) {
         SERVE_TRY(cudaMemcpyAsync(s.d2, s.h2.data(), n2 * sizeof(BatchGrid), cudaMemcpyHostToDevice, s.s2));
-        SERVE_TRY(upload_map(s.map2, &s.d_map2, &s.cap_map2, s.s2));
-        const int depth = s.depth2d;
-        const size_t smem = stencil2d_tb_smem<float>(1, depth);
-        auto rk = batch_round_kernel<float>;
-        if (smem > 48 * 1024) SERVE_TRY(cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        int per_sm = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rk, kSt2Threads, smem);
-        const long long grid = std::max(1LL, std::min<long long>(tiles, (long long)std::max(per_sm, 1) * s.sm_count));
-        const int launches = s.check_every / depth;
-        for (int j = 0; j < launches; j++) {
-            const int check = j == launches - 1;
-            rk<<<(unsigned)grid, kSt2Threads, smem, s.s2>>>(s.d2, s.dlist, s.d_map2, tiles, depth, check);
-            batch_finalize_kernel<<<1, 256, 0, s.s2>>>(s.d2, s.dlist, n2, depth, check, s.tol, s.max_iters,
-                                                        s.d_active);
+        if (nres) {  // resident grids on their own stream, overlapping the work-list rounds
+            SERVE_TRY(cudaEventRecord(s.ev_res_fork, s.s2));
+            SERVE_TRY(cudaStreamWaitEvent(s.sr, s.ev_res_fork, 0));
+            auto k = batch_resident_kernel<float>;
+            SERVE_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)res_smem));
+            k<<<(unsigned)nres, kBatchResidentThreads, res_smem, s.sr>>>(s.d2, s.dlist + nw, s.tol, s.max_iters,
+                                                                          s.check_every, s.check_every);
+            SERVE_TRY(cudaGetLastError());
+            rt::count_launch();
+            SERVE_TRY(cudaEventRecord(s.ev_res_join, s.sr));
         }
-        SERVE_TRY(cudaGetLastError());
-        rt::count_launch(2 * launches);
+        if (tiles) {
+            SERVE_TRY(upload_map(s.map2, &s.d_map2, &s.cap_map2, s.s2));
+            const int depth = s.depth2d;
+            const size_t smem = stencil2d_tb_smem<float>(1, depth);
+            auto rk = batch_round_kernel<float>;
+            if (smem > 48 * 1024)
+                SERVE_TRY(cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            int per_sm = 1;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rk, kSt2Threads, smem);
+            const long long grid =
+                std::max(1LL, std::min<long long>(tiles, (long long)std::max(per_sm, 1) * s.sm_count));
+            const int launches = s.check_every / depth;
+            for (int j = 0; j < launches; j++) {
+                const int check = j == launches - 1;
+                rk<<<(unsigned)grid, kSt2Threads, smem, s.s2>>>(s.d2, s.dlist, s.d_map2, tiles, depth, check,
+                                                                 s.d_ticket, nw, s.tol, s.max_iters, s.d_active);
+            }
+            SERVE_TRY(cudaGetLastError());
+            rt::count_launch(launches);
+        }
+        if (nres) SERVE_TRY(cudaStreamWaitEvent(s.s2, s.ev_res_join, 0));
         SERVE_TRY(cudaMemcpyAsync(s.h2.data(), s.d2, n2 * sizeof(BatchGrid), cudaMemcpyDeviceToHost, s.s2));
     }
     if (n3) {
@@ -220,11 +255,11 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
         const long long grid = std::max(1LL, std::min<long long>(blocks, (long long)std::max(per_sm, 1) * s.sm_count));
         for (int j = 0; j < s.check_every; j++) {
             const int check = j == s.check_every - 1;
-            serve3d_round_kernel<<<(unsigned)grid, kT3Threads, smem, s.s3>>>(s.d3, s.dlist, s.d_map3, blocks, check);
-            serve3d_finalize_kernel<<<1, 256, 0, s.s3>>>(s.d3, s.dlist, n3, check, s.tol, s.max_iters);
+            serve3d_round_kernel<<<(unsigned)grid, kT3Threads, smem, s.s3>>>(s.d3, s.dlist, s.d_map3, blocks, check,
+                                                                             s.d_ticket + 1, n3, s.tol, s.max_iters);
         }
         SERVE_TRY(cudaGetLastError());
-        rt::count_launch(2 * s.check_every);
+        rt::count_launch(s.check_every);
         SERVE_TRY(cudaMemcpyAsync(s.h3.data(), s.d3, n3 * sizeof(ServeCube), cudaMemcpyDeviceToHost, s.s3));
     }
     SERVE_TRY(cudaEventRecord(s.ev_join, s.s3));
@@ -245,6 +280,45 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
         r->finished = s.h3[i].done != 0;
     }
     return cudaSuccess;
+}
+
+// The running requests one check interval advances. Running every request in
+// every interval makes a small request wait for as many intervals as the
+// largest one needs, each as long as the sum of all requests' sweeps; so an
+// interval takes the requests with the smallest remaining work (cells times
+// sweeps left before the cap) until kIntervalCells cells are scheduled --
+// several waves of blocks, enough to fill the GPU. A request left out ages:
+// its priority is its remaining work halved for every kAgeHalving intervals
+// it waited, so large requests keep moving under a steady stream of small
+// ones. Which requests share an interval changes only the order in which
+// sweeps happen, never a request's own sweeps, so results are unchanged.
+constexpr size_t kIntervalCells = 48ull << 20;
+constexpr double kAgeHalving = 16.0;
+
+std::vector<Request *> pick_interval(Server &s, const std::vector<Request *> &running) {
+    std::vector<std::pair<double, Request *>> order;
+    order.reserve(running.size());
+    for (Request *r : running) {
+        const double rem = (double)r->cells() * (double)std::max(1LL, s.max_iters - r->iters);
+        order.emplace_back(rem * std::exp2(-r->waited / kAgeHalving), r);
+    }
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<double, Request *> &a, const std::pair<double, Request *> &b) {
+                         return a.first < b.first;
+                     });
+    std::vector<Request *> pick;
+    size_t cells = 0;
+    for (auto &pr : order) {
+        Request *r = pr.second;
+        if (!pick.empty() && cells >= kIntervalCells) {
+            r->waited++;
+            continue;
+        }
+        pick.push_back(r);
+        cells += r->cells();
+        r->waited = 0;
+    }
+    return pick;
 }
 
 // Called by the worker with the lock held and no device work in flight.
@@ -354,6 +428,7 @@ void worker_loop(Server *sp) {
             }
         }
         if (ok) {
+            act = pick_interval(s, act);
             cudaError_t e = run_interval(s, act);
             if (e != cudaSuccess) {
                 ok = false;
@@ -423,6 +498,11 @@ int msl_server_start(size_t hbm_budget, double tol, long long max_iters, int che
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s3, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->sr, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_res_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_res_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_ticket, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(s->d_ticket, 0, 2 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc(&s->d2, kMaxActive * sizeof(BatchGrid));
     if (e == cudaSuccess) e = cudaMalloc(&s->d3, kMaxActive * sizeof(ServeCube));
     if (e == cudaSuccess) e = cudaMalloc(&s->dlist, kMaxActive * sizeof(int));
@@ -642,8 +722,12 @@ int msl_server_stop(void *server) {
     cudaFree(s->d_active);
     if (s->d_map2) cudaFree(s->d_map2);
     if (s->d_map3) cudaFree(s->d_map3);
+    cudaFree(s->d_ticket);
     cudaEventDestroy(s->ev_fork);
     cudaEventDestroy(s->ev_join);
+    cudaEventDestroy(s->ev_res_fork);
+    cudaEventDestroy(s->ev_res_join);
+    cudaStreamDestroy(s->sr);
     cudaStreamDestroy(s->s2);
     cudaStreamDestroy(s->s3);
     std::string err = s->error;

@@ -35,6 +35,50 @@ struct BatchGrid {
     long long first_tile;   // prefix of tile counts (work-list grids only)
 };
 
+// True in every thread of the CTA that finishes last among the launch's CTAs
+// (a ticket taken after a fence, so the other CTAs' writes are visible to
+// it); that CTA resets the ticket for the next launch.
+MSL_DEV bool last_cta_arrives(unsigned *ticket) {
+    __shared__ int s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        if (threadIdx.x == 0) *ticket = 0u;
+    }
+    return s_last != 0;
+}
+
+// After a round: advance the sweep counts and, on a check round, take the
+// residuals and retire converged grids (and grids out of sweeps). Counts the
+// grids still running into *active. Run by one whole CTA.
+MSL_DEV void batch_finalize_body(BatchGrid *grids, const int *list, int nlist, int depth, int check, double tol,
+                                 long long max_iters, int *active) {
+    __shared__ int s_active;
+    if (threadIdx.x == 0) s_active = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nlist; i += blockDim.x) {
+        BatchGrid &g = grids[list[i]];
+        if (g.done) continue;
+        g.iters += depth;
+        g.cur ^= 1;
+        if (check) {
+            double r = __longlong_as_double((long long)g.resid_bits);
+            g.residual = r;
+            g.resid_bits = 0ull;
+            if (!(r > tol)) g.done = 1;
+        }
+        if (g.iters >= max_iters) g.done = 1;
+        if (!g.done) atomicAdd(&s_active, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *active = s_active;
+}
+
 // The plain-Jacobi functor: boundary cells keep their value, inside cells
 // take (((0 + W) + E) + N) + S times 0.25 (heatdiffusion order; x*0.25 == x/4).
 struct JacobiFn {
@@ -57,11 +101,13 @@ struct JacobiFn {
 constexpr int kBatchResidentThreads = 512;
 
 // One CTA per grid in `list`: load the latest iterate into shared memory,
-// sweep until the residual check passes or max_iters sweeps are done, store
-// the result into buf[0].
+// sweep until the residual check passes, max_iters sweeps are done or this
+// launch's max_sweeps have run (a multiple of check_every), store the result
+// into buf[0].
 template <typename S>
 __global__ void __launch_bounds__(kBatchResidentThreads)
-    batch_resident_kernel(BatchGrid *grids, const int *list, double tol, long long max_iters, int check_every) {
+    batch_resident_kernel(BatchGrid *grids, const int *list, double tol, long long max_iters, int check_every,
+                          long long max_sweeps) {
     using T = typename Compute<S>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     BatchGrid &g = grids[list[blockIdx.x]];
@@ -87,10 +133,12 @@ __global__ void __launch_bounds__(kBatchResidentThreads)
     JacobiFn fn;
     int c = 0;
     long long it = g.iters;  // a multiple of check_every: checks stay on the same sweeps
+    const long long it_end = max_sweeps < max_iters - it ? it + max_sweeps : max_iters;  // this launch's sweeps
     double res = g.residual;
+    bool converged = false;
     __shared__ int s_stop;
-    while (it < max_iters) {
-        const long long k = min((long long)check_every, max_iters - it);
+    while (it < it_end) {
+        const long long k = min((long long)check_every, it_end - it);
         double dmax = 0.0;
         for (long long s = 0; s < k; s++) {
             m.tile_ = bufs[c];
@@ -115,7 +163,10 @@ __global__ void __launch_bounds__(kBatchResidentThreads)
             s_stop = !(dmax > tol);  // NaN keeps iterating until max_iters
         }
         __syncthreads();
-        if (s_stop) break;
+        if (s_stop) {
+            converged = true;
+            break;
+        }
     }
     S *dst_g = (S *)g.buf[0];
     for (int i = threadIdx.x; i < n; i += blockDim.x) dst_g[i] = bufs[c][i];
@@ -123,7 +174,7 @@ __global__ void __launch_bounds__(kBatchResidentThreads)
         g.cur = 0;
         g.iters = it;
         g.residual = res;
-        g.done = 1;
+        g.done = converged || it >= max_iters;
     }
 }
 
@@ -135,7 +186,7 @@ __global__ void __launch_bounds__(kBatchResidentThreads)
 template <typename S>
 __global__ void __launch_bounds__(kSt2Threads)
     batch_round_kernel(BatchGrid *grids, const int *list, const int *tile_grid, long long total_tiles, int depth,
-                       int check) {
+                       int check, unsigned *ticket, int nlist, double tol, long long max_iters, int *active) {
     using T = typename Compute<S>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int r = 1;
@@ -151,8 +202,8 @@ __global__ void __launch_bounds__(kSt2Threads)
         if (g.done) continue;  // uniform for the CTA
         const int rows = g.rows, cols = g.cols;
         const int tiles_x = (cols + kSt2BX - 1) / kSt2BX;
-        const long long t = item - g.first_tile;
-        const int x0 = (int)(t % tiles_x) * kSt2BX, y0 = (int)(t / tiles_x) * kSt2BY;
+        const unsigned t = (unsigned)(item - g.first_tile);  // < 2^30 cells / 2048 per tile
+        const int x0 = (int)(t % (unsigned)tiles_x) * kSt2BX, y0 = (int)(t / (unsigned)tiles_x) * kSt2BY;
         const S *in = (const S *)g.buf[g.cur];
         S *out = (S *)g.buf[g.cur ^ 1];
         const int wx0 = x0 - hx, wy0 = y0 - depth * r;
@@ -186,32 +237,14 @@ __global__ void __launch_bounds__(kSt2Threads)
             if (threadIdx.x == 0) atomic_max_nonneg(&g.resid_bits, dmax);
         }
     }
+    // With a ticket the last CTA to finish also does batch_finalize's work
+    // (one launch per round instead of two).
+    if (ticket && last_cta_arrives(ticket)) batch_finalize_body(grids, list, nlist, depth, check, tol, max_iters, active);
 }
 
-// After a round: advance the sweep counts and, on a check round, take the
-// residuals and retire converged grids (and grids out of sweeps). Counts the
-// grids still running into *active.
 static __global__ void batch_finalize_kernel(BatchGrid *grids, const int *list, int nlist, int depth,
                                       int check, double tol, long long max_iters, int *active) {
-    __shared__ int s_active;
-    if (threadIdx.x == 0) s_active = 0;
-    __syncthreads();
-    for (int i = threadIdx.x; i < nlist; i += blockDim.x) {
-        BatchGrid &g = grids[list[i]];
-        if (g.done) continue;
-        g.iters += depth;
-        g.cur ^= 1;
-        if (check) {
-            double r = __longlong_as_double((long long)g.resid_bits);
-            g.residual = r;
-            g.resid_bits = 0ull;
-            if (!(r > tol)) g.done = 1;
-        }
-        if (g.iters >= max_iters) g.done = 1;
-        if (!g.done) atomicAdd(&s_active, 1);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) *active = s_active;
+    batch_finalize_body(grids, list, nlist, depth, check, tol, max_iters, active);
 }
 
 }  // namespace gpu

@@ -2,8 +2,10 @@
 // 2-D rounds (msl_batch.cuh). Every active heat3D request's cube is cut into
 // 64 x 16 x 8 blocks; a persistent kernel takes (request, block) items
 // round-robin and advances each block one sweep (buf[cur] -> buf[cur ^ 1]);
-// serve3d_finalize then advances the sweep counts and, on check sweeps, takes
-// the per-request FP64 residuals. 2-D Jacobi requests use batch_round_kernel.
+// the last CTA of each launch then advances the sweep counts and, on check
+// sweeps, takes the per-request FP64 residuals. 2-D Jacobi requests use
+// batch_round_kernel (same fused finalize) and, when both iterates fit in
+// shared memory, batch_resident_kernel (one launch per check interval).
 #pragma once
 
 #include "msl_batch.cuh"
@@ -39,8 +41,28 @@ struct Heat7Fn {
     }
 };
 
+// After a sweep: advance the sweep counts and, on a check sweep, take the
+// residuals and retire converged cubes. Run by one whole CTA.
+MSL_DEV void serve3d_finalize_body(ServeCube *cubes, const int *list, int nlist, int check, double tol,
+                                   long long max_iters) {
+    for (int i = threadIdx.x; i < nlist; i += blockDim.x) {
+        ServeCube &cb = cubes[list[i]];
+        if (cb.done) continue;
+        cb.iters += 1;
+        cb.cur ^= 1;
+        if (check) {
+            const double r = __longlong_as_double((long long)cb.resid_bits);
+            cb.residual = r;
+            cb.resid_bits = 0ull;
+            if (!(r > tol)) cb.done = 1;
+        }
+        if (cb.iters >= max_iters) cb.done = 1;
+    }
+}
+
 static __global__ void __launch_bounds__(kT3Threads, 3)
-    serve3d_round_kernel(ServeCube *cubes, const int *list, const int *block_cube, long long total_blocks, int check) {
+    serve3d_round_kernel(ServeCube *cubes, const int *list, const int *block_cube, long long total_blocks, int check,
+                         unsigned *ticket, int nlist, double tol, long long max_iters) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float *box = reinterpret_cast<float *>(smem_raw + kStHeader);
     const int r = 1, hx = halo_x<float>(1);
@@ -52,8 +74,9 @@ static __global__ void __launch_bounds__(kT3Threads, 3)
         if (cb.done) continue;  // uniform for the CTA
         const int depth = cb.depth, rows = cb.rows, cols = cb.cols;
         const int bx = (cols + kT3BX - 1) / kT3BX, by = (rows + kT3BY - 1) / kT3BY;
-        const long long b = item - cb.first_block;
-        const int x0 = (int)(b % bx) * kT3BX, y0 = (int)((b / bx) % by) * kT3BY, z0 = (int)(b / ((long long)bx * by)) * kT3BZ;
+        const unsigned b = (unsigned)(item - cb.first_block);  // < 2^31 cells / 8192 per block
+        const unsigned bxy = (unsigned)bx * (unsigned)by, bz = b / bxy, rem = b - bz * bxy, byy = rem / (unsigned)bx;
+        const int x0 = (int)(rem - byy * (unsigned)bx) * kT3BX, y0 = (int)byy * kT3BY, z0 = (int)bz * kT3BZ;
         const float *in = (const float *)cb.buf[cb.cur];
         float *out = (float *)cb.buf[cb.cur ^ 1];
         const int wx0 = x0 - hx, wy0 = y0 - r, wz0 = z0 - r;
@@ -78,23 +101,8 @@ static __global__ void __launch_bounds__(kT3Threads, 3)
             if (threadIdx.x == 0) atomic_max_nonneg(&cb.resid_bits, dmax);
         }
     }
-}
-
-static __global__ void serve3d_finalize_kernel(ServeCube *cubes, const int *list, int nlist, int check, double tol,
-                                        long long max_iters) {
-    for (int i = threadIdx.x; i < nlist; i += blockDim.x) {
-        ServeCube &cb = cubes[list[i]];
-        if (cb.done) continue;
-        cb.iters += 1;
-        cb.cur ^= 1;
-        if (check) {
-            const double r = __longlong_as_double((long long)cb.resid_bits);
-            cb.residual = r;
-            cb.resid_bits = 0ull;
-            if (!(r > tol)) cb.done = 1;
-        }
-        if (cb.iters >= max_iters) cb.done = 1;
-    }
+    // The last CTA to finish advances the counts (one launch per sweep).
+    if (last_cta_arrives(ticket)) serve3d_finalize_body(cubes, list, nlist, check, tol, max_iters);
 }
 
 inline size_t serve3d_smem() {

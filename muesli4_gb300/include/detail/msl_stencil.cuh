@@ -256,36 +256,29 @@ MSL_DEV void tb_inner_sweeps(const Fn &fn, NPLMatrix<typename Compute<S>::type, 
         if (interior) {
             m.check_ = false;
             if constexpr (has_strip2<Fn>::value) {
-                // The block's own 64 columns in whole kSt2RPT-row strips
-                // through the functor's strip() (two full warps per strip
-                // row)...
-                const int nstrips = H / kSt2RPT, sr = nstrips * kSt2RPT;
-                for (int item = warp; item < 2 * nstrips; item += nwarps) {
-                    const int sidx = item >> 1, col = ext + (item & 1) * 32 + lane;
+                // Whole kSt2RPT-row strips through the functor's strip(): the
+                // strips start every kSt2RPT rows and the last one is moved
+                // up to end at row H (it recomputes a few rows of the one
+                // before; both write the same values, as every cell is a
+                // function of the source buffer alone). The block's own 64
+                // columns take two full warps per strip row; the ext-wide
+                // side columns one thread per strip, from the last threads
+                // of the CTA (whose warps have fewer central strips).
+                const int ns = (H + kSt2RPT - 1) / kSt2RPT;
+                auto strip_at = [&](int col, int sidx) {
+                    const int row0 = min(sidx * kSt2RPT, H - kSt2RPT);
                     T vals[kSt2RPT];
-                    const int gx = gx0 + col, gy = gy0 + sidx * kSt2RPT;
+                    const int gx = gx0 + col, gy = gy0 + row0;
                     fn.strip(m, gx, gy, vals);
                     S *d = dst + (gy - wy0) * pitch + (gx - wx0);
 #pragma unroll
                     for (int j = 0; j < kSt2RPT; j++) d[j * pitch] = narrow<S>(vals[j]);
-                }
-                // ...then the margin cells spread over all threads: the two
-                // ext-wide side columns (rows 0..H-1), then the rows below the
-                // strips.
-                const int side = ext * H, total = 2 * side + (H - sr) * kSt2BX;
-                for (int t = threadIdx.x; t < total; t += blockDim.x) {
-                    int row, col;
-                    if (t < 2 * side) {
-                        const int u = t < side ? t : t - side, rr = u / ext;
-                        row = rr;
-                        col = (t < side ? 0 : ext + kSt2BX) + (u - rr * ext);
-                    } else {
-                        const int u = t - 2 * side;
-                        row = sr + u / kSt2BX;
-                        col = ext + u % kSt2BX;
-                    }
-                    const int gx = gx0 + col, gy = gy0 + row;
-                    dst[(gy - wy0) * pitch + (gx - wx0)] = narrow<S>(fn(m, gx, gy));
+                };
+                for (int item = warp; item < 2 * ns; item += nwarps) strip_at(ext + (item & 1) * 32 + lane, item >> 1);
+                const int side = 2 * ext;
+                for (int t = (int)blockDim.x - 1 - (int)threadIdx.x; t < side * ns; t += blockDim.x) {
+                    const int sidx = t / side, c = t - sidx * side;
+                    strip_at(c < ext ? c : kSt2BX + c, sidx);
                 }
             } else {
                 sweep_cells(m);
