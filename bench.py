@@ -658,6 +658,11 @@ def run_serve(args, dist: Dist):
             cache[i] = np.random.default_rng(sd).random(shape, dtype=np.float32)
         return cache[i]
 
+    # The autotuner picks the 2-D temporal depth per grid-size class; the plain
+    # path and the server both use its records.
+    tuned = {}
+    for n in (256, 512, 1024, 2048, 4096):
+        tuned[n], _ = A.autotune_stencil2d(A.MSL_ST2_JACOBI5, A.MSL_F32, n, n, 1, 100)
     # plain path: service time of a sample of requests, one at a time
     rng = np.random.default_rng(5)
     sample = sorted(rng.choice(len(reqs), size=min(args.serve_plain_sample, len(reqs)), replace=False).tolist())
@@ -721,7 +726,8 @@ def run_serve(args, dist: Dist):
                 "config": {"workload": f"{len(reqs)} requests: half 2-D Jacobi n^2 (n log-uniform [64,4096]), half "
                                        f"3-D heat m^3 (m log-uniform [32,256]); U[0,1) init; residual <= {tol} "
                                        f"every {check} sweeps or {cap} sweeps; HBM budget 120 GB; Poisson arrivals",
-                           "plain_capacity_per_s": plain_capacity, "plain_sample": len(service)},
+                           "plain_capacity_per_s": plain_capacity, "plain_sample": len(service),
+                           "jacobi_temporal_depth_by_side": tuned},
                 "sweep": sweep, "served_over_plain_at_top_rate": top["served_solves_per_s"] / top["plain_solves_per_s"]}
         print(json.dumps(line), flush=True)
 

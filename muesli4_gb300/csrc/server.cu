@@ -82,6 +82,7 @@ struct Server {
     cudaStream_t s2 = nullptr, s3 = nullptr, sr = nullptr;  // 2-D rounds, 3-D rounds, resident 2-D grids
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_res_fork = nullptr, ev_res_join = nullptr;
     unsigned *d_ticket = nullptr;  // last-CTA tickets of the 2-D and 3-D round kernels
+    unsigned *d_err = nullptr, *h_err = nullptr;  // error word of the one-request kernels (device, pinned host)
     BatchGrid *d2 = nullptr;
     ServeCube *d3 = nullptr;
     int *dlist = nullptr;  // 0..kMaxActive-1
@@ -118,6 +119,12 @@ struct CkptRecord {
     double residual;
 };
 static_assert(sizeof(CkptHeader) == 48 && sizeof(CkptRecord) == 48, "checkpoint layout");
+
+double bits_to_double(unsigned long long bits) {
+    double d;
+    std::memcpy(&d, &bits, sizeof d);
+    return d;
+}
 
 size_t iterate_bytes(const Request &r) { return 2 * ((r.cells() * sizeof(float) + 255) / 256 * 256); }
 
@@ -158,6 +165,17 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
     std::vector<Request *> r2, r3, res2;
     long long tiles = 0, blocks = 0;
     size_t res_smem = 0;
+    auto cube3d = [](const Request *r) {
+        ServeCube c{};
+        c.buf[0] = r->buf[0];
+        c.buf[1] = r->buf[1];
+        c.depth = r->depth;
+        c.rows = r->rows;
+        c.cols = r->cols;
+        c.cur = r->cur;
+        c.iters = r->iters;
+        return c;
+    };
     auto grid2d = [](const Request *r) {
         BatchGrid g{};
         g.buf[0] = r->buf[0];
@@ -168,12 +186,19 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
         g.iters = r->iters;
         return g;
     };
+    std::vector<Request *> big2, big3;
+    const long long big_items = 2LL * s.sm_count;  // a request this large fills the GPU on its own
     for (Request *r : act) {
         if (r->kind == MSL_SERVE_JACOBI2D) {
             const size_t need = 2 * ((r->cells() * sizeof(float) + 127) / 128 * 128);
             if (need <= kResidentSmem) {  // whole grid in shared memory: one launch per interval
                 res2.push_back(r);
                 res_smem = std::max(res_smem, need);
+                continue;
+            }
+            const long long nt0 = (long long)((r->cols + kSt2BX - 1) / kSt2BX) * ((r->rows + kSt2BY - 1) / kSt2BY);
+            if (nt0 >= big_items) {  // the one-request kernels (TMA, temporal blocking)
+                big2.push_back(r);
                 continue;
             }
             BatchGrid g = grid2d(r);
@@ -184,29 +209,38 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
             s.h2.push_back(g);
             r2.push_back(r);
         } else {
-            ServeCube c{};
-            c.buf[0] = r->buf[0];
-            c.buf[1] = r->buf[1];
-            c.depth = r->depth;
-            c.rows = r->rows;
-            c.cols = r->cols;
-            c.cur = r->cur;
-            c.iters = r->iters;
-            c.first_block = blocks;
             const long long nb = (long long)((r->cols + kT3BX - 1) / kT3BX) * ((r->rows + kT3BY - 1) / kT3BY) *
                                  ((r->depth + kT3BZ - 1) / kT3BZ);
+            if (nb >= big_items) {
+                big3.push_back(r);
+                continue;
+            }
+            ServeCube c = cube3d(r);
+            c.first_block = blocks;
             blocks += nb;
             s.map3.insert(s.map3.end(), (size_t)nb, (int)s.h3.size());
             s.h3.push_back(c);
             r3.push_back(r);
         }
     }
-    const int nw = (int)s.h2.size();  // work-list grids first, then the resident ones
+    // descriptor order: batched grids first (the fused finalize covers them),
+    // then the resident 2-D grids, then the large requests (their descriptors
+    // only carry the residual slot)
+    const int nw = (int)s.h2.size(), n3b = (int)s.h3.size();
     for (Request *r : res2) {
         s.h2.push_back(grid2d(r));
         r2.push_back(r);
     }
-    const int n2 = (int)s.h2.size(), n3 = (int)s.h3.size(), nres = n2 - nw;
+    const int nres = (int)s.h2.size() - nw;
+    for (Request *r : big2) {
+        s.h2.push_back(grid2d(r));
+        r2.push_back(r);
+    }
+    for (Request *r : big3) {
+        s.h3.push_back(cube3d(r));
+        r3.push_back(r);
+    }
+    const int n2 = (int)s.h2.size(), n3 = (int)s.h3.size();
     SERVE_TRY(cudaEventRecord(s.ev_fork, s.s2));
     SERVE_TRY(cudaStreamWaitEvent(s.s3, s.ev_fork, 0));
     if (n2) {
@@ -242,31 +276,79 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
             SERVE_TRY(cudaGetLastError());
             rt::count_launch(launches);
         }
+        for (size_t k = 0; k < big2.size(); k++) {  // as msl_stencil2d_iterate runs a grid alone
+            Request *r = big2[k];
+            BatchGrid *dg = s.d2 + nw + nres + (int)k;
+            const int depth = rt::tuned_depth(MSL_F32, MSL_ST2_JACOBI5, r->rows, r->cols, 1);
+            float *p = (float *)r->buf[r->cur], *q = (float *)r->buf[r->cur ^ 1];
+            for (int i = 0; i < s.check_every;) {
+                const int d = std::min(std::max(depth, 1), s.check_every - i);
+                unsigned long long *resid = i + d == s.check_every ? &dg->resid_bits : nullptr;
+                cudaError_t e = d > 1 ? launch_stencil2d_tb<float>(p, q, r->rows, r->cols, 1, d, 0.0f, JacobiFn{}, resid,
+                                                                   s.d_err, s.s2)
+                                      : launch_stencil2d<float>(p, q, r->rows, r->cols, 1, 0.0f, JacobiFn{}, resid,
+                                                                s.d_err, s.s2);
+                SERVE_TRY(e);
+                rt::count_launch();
+                std::swap(p, q);
+                i += d;
+            }
+        }
         if (nres) SERVE_TRY(cudaStreamWaitEvent(s.s2, s.ev_res_join, 0));
         SERVE_TRY(cudaMemcpyAsync(s.h2.data(), s.d2, n2 * sizeof(BatchGrid), cudaMemcpyDeviceToHost, s.s2));
     }
     if (n3) {
         SERVE_TRY(cudaMemcpyAsync(s.d3, s.h3.data(), n3 * sizeof(ServeCube), cudaMemcpyHostToDevice, s.s3));
-        SERVE_TRY(upload_map(s.map3, &s.d_map3, &s.cap_map3, s.s3));
-        const size_t smem = serve3d_smem();
-        SERVE_TRY(cudaFuncSetAttribute(serve3d_round_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        int per_sm = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, serve3d_round_kernel, kT3Threads, smem);
-        const long long grid = std::max(1LL, std::min<long long>(blocks, (long long)std::max(per_sm, 1) * s.sm_count));
-        for (int j = 0; j < s.check_every; j++) {
-            const int check = j == s.check_every - 1;
-            serve3d_round_kernel<<<(unsigned)grid, kT3Threads, smem, s.s3>>>(s.d3, s.dlist, s.d_map3, blocks, check,
-                                                                             s.d_ticket + 1, n3, s.tol, s.max_iters);
+        if (blocks) {
+            SERVE_TRY(upload_map(s.map3, &s.d_map3, &s.cap_map3, s.s3));
+            const size_t smem = serve3d_smem();
+            SERVE_TRY(cudaFuncSetAttribute(serve3d_round_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            int per_sm = 1;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, serve3d_round_kernel, kT3Threads, smem);
+            const long long grid =
+                std::max(1LL, std::min<long long>(blocks, (long long)std::max(per_sm, 1) * s.sm_count));
+            for (int j = 0; j < s.check_every; j++) {
+                const int check = j == s.check_every - 1;
+                serve3d_round_kernel<<<(unsigned)grid, kT3Threads, smem, s.s3>>>(
+                    s.d3, s.dlist, s.d_map3, blocks, check, s.d_ticket + 1, n3b, s.tol, s.max_iters);
+            }
+            SERVE_TRY(cudaGetLastError());
+            rt::count_launch(s.check_every);
         }
-        SERVE_TRY(cudaGetLastError());
-        rt::count_launch(s.check_every);
+        for (size_t k = 0; k < big3.size(); k++) {  // as msl_stencil3d_iterate runs a cube alone
+            Request *r = big3[k];
+            ServeCube *dc = s.d3 + n3b + (int)k;
+            float *p = (float *)r->buf[r->cur], *q = (float *)r->buf[r->cur ^ 1];
+            for (int i = 0; i < s.check_every; i++) {
+                unsigned long long *resid = i + 1 == s.check_every ? &dc->resid_bits : nullptr;
+                SERVE_TRY(launch_stencil3d<float>(p, q, r->depth, r->rows, r->cols, 1, 0.0f, Heat7Fn{}, resid, s.d_err,
+                                                  s.s3, s.sm_count));
+                rt::count_launch();
+                std::swap(p, q);
+            }
+        }
         SERVE_TRY(cudaMemcpyAsync(s.h3.data(), s.d3, n3 * sizeof(ServeCube), cudaMemcpyDeviceToHost, s.s3));
     }
     SERVE_TRY(cudaEventRecord(s.ev_join, s.s3));
     SERVE_TRY(cudaStreamWaitEvent(s.s2, s.ev_join, 0));
+    if (!big2.empty() || !big3.empty())
+        SERVE_TRY(cudaMemcpyAsync(s.h_err, s.d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s.s2));
     SERVE_TRY(cudaStreamSynchronize(s.s2));
+    if (*s.h_err) return cudaErrorLaunchTimeout;  // a bounded wait in a stencil kernel gave up
+    // large requests: one check interval of sweeps, the residual of its last sweep
+    auto advance = [&](Request *r, unsigned long long bits, int flips) {
+        r->iters += s.check_every;
+        r->cur ^= flips & 1;
+        r->residual = bits_to_double(bits);
+        r->finished = !(r->residual > s.tol) || r->iters >= s.max_iters;
+    };
     for (int i = 0; i < n2; i++) {
         Request *r = r2[i];
+        if (i >= nw + nres) {
+            const int depth = std::max(1, rt::tuned_depth(MSL_F32, MSL_ST2_JACOBI5, r->rows, r->cols, 1));
+            advance(r, s.h2[i].resid_bits, (s.check_every + depth - 1) / depth);
+            continue;
+        }
         r->cur = s.h2[i].cur;
         r->iters = s.h2[i].iters;
         r->residual = s.h2[i].residual;
@@ -274,6 +356,10 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
     }
     for (int i = 0; i < n3; i++) {
         Request *r = r3[i];
+        if (i >= n3b) {
+            advance(r, s.h3[i].resid_bits, s.check_every);
+            continue;
+        }
         r->cur = s.h3[i].cur;
         r->iters = s.h3[i].iters;
         r->residual = s.h3[i].residual;
@@ -503,6 +589,10 @@ int msl_server_start(size_t hbm_budget, double tol, long long max_iters, int che
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_res_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_ticket, 2 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(s->d_ticket, 0, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_err, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(s->d_err, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_err, sizeof(unsigned));
+    if (e == cudaSuccess) *s->h_err = 0;
     if (e == cudaSuccess) e = cudaMalloc(&s->d2, kMaxActive * sizeof(BatchGrid));
     if (e == cudaSuccess) e = cudaMalloc(&s->d3, kMaxActive * sizeof(ServeCube));
     if (e == cudaSuccess) e = cudaMalloc(&s->dlist, kMaxActive * sizeof(int));
@@ -723,6 +813,8 @@ int msl_server_stop(void *server) {
     if (s->d_map2) cudaFree(s->d_map2);
     if (s->d_map3) cudaFree(s->d_map3);
     cudaFree(s->d_ticket);
+    cudaFree(s->d_err);
+    cudaFreeHost(s->h_err);
     cudaEventDestroy(s->ev_fork);
     cudaEventDestroy(s->ev_join);
     cudaEventDestroy(s->ev_res_fork);

@@ -114,20 +114,53 @@ template <typename S> MSL_HD int halo_x(int r) {
 
 // Stage a window of `nrows` rows (pitch elements each) with plain coalesced
 // loads: window row k is grid row (wy0 + k % th) of plane (wz0 + k / th); the
-// elements outside the grid become zero. One warp per window row, so the row
-// and plane come from one division per row rather than per element.
+// elements outside the grid become zero. Each warp takes kStageRows rows at a
+// time and every lane issues all of its loads for them (up to kStageRows x
+// kStageCols) before the first store, so the loads' latencies overlap instead
+// of adding up row after row. Windows wider than 32 * kStageCols take a
+// row-at-a-time loop.
+constexpr int kStageRows = 4, kStageCols = 4;
+
 template <typename S>
 MSL_DEV void stage_window(S *dst, const S *in, int pitch, int th, int nrows, int wx0, int wy0, int wz0, int depth,
                           int rows, int cols) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int k = warp; k < nrows; k += nwarps) {
+    auto row_src = [&](int k, bool &row_in) {
         const int zz = k / th, gy = wy0 + (k - zz * th), gz = wz0 + zz;
-        const bool row_in = gy >= 0 && gy < rows && gz >= 0 && gz < depth;
-        const S *src = in + ((size_t)(row_in ? gz : 0) * rows + (row_in ? gy : 0)) * cols;
-        S *d = dst + (size_t)k * pitch;
-        for (int xx = lane; xx < pitch; xx += 32) {
-            const int gx = wx0 + xx;
-            d[xx] = (row_in && gx >= 0 && gx < cols) ? src[gx] : S{};
+        row_in = gy >= 0 && gy < rows && gz >= 0 && gz < depth;
+        return in + ((size_t)(row_in ? gz : 0) * rows + (row_in ? gy : 0)) * cols;
+    };
+    if (pitch > 32 * kStageCols) {
+        for (int k = warp; k < nrows; k += nwarps) {
+            bool row_in;
+            const S *src = row_src(k, row_in);
+            S *d = dst + (size_t)k * pitch;
+            for (int xx = lane; xx < pitch; xx += 32) {
+                const int gx = wx0 + xx;
+                d[xx] = (row_in && gx >= 0 && gx < cols) ? src[gx] : S{};
+            }
+        }
+        return;
+    }
+    for (int k0 = warp * kStageRows; k0 < nrows; k0 += nwarps * kStageRows) {
+        S v[kStageRows][kStageCols];
+#pragma unroll
+        for (int u = 0; u < kStageRows; u++) {
+            bool row_in = false;
+            const S *src = k0 + u < nrows ? row_src(k0 + u, row_in) : in;
+#pragma unroll
+            for (int q = 0; q < kStageCols; q++) {
+                const int xx = lane + 32 * q, gx = wx0 + xx;
+                v[u][q] = (row_in && xx < pitch && gx >= 0 && gx < cols) ? src[gx] : S{};
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kStageRows; u++) {
+            if (k0 + u >= nrows) break;
+            S *d = dst + (size_t)(k0 + u) * pitch;
+#pragma unroll
+            for (int q = 0; q < kStageCols; q++)
+                if (lane + 32 * q < pitch) d[lane + 32 * q] = v[u][q];
         }
     }
 }

@@ -28,7 +28,8 @@ def plain(gpu, init):
     return out.download(), it, res
 
 
-SHAPES = [(64, 64), (100, 300), (257, 129), (16, 16, 16), (24, 40, 70), (33, 17, 64), (512, 512), (40, 40, 40)]
+SHAPES = [(64, 64), (100, 300), (257, 129), (16, 16, 16), (24, 40, 70), (33, 17, 64), (512, 512), (40, 40, 40),
+          (1024, 1024), (72, 160, 128)]  # the last two fill the GPU alone: one-request kernels
 
 
 def assert_same(got, want):
