@@ -250,7 +250,7 @@ class StencilSuite:
         # iterated 2-D part; its records are used by the timed iterate calls.
         self.tuned = {}
         if "life" in self.parts:
-            d, rate = A.autotune_stencil2d(A.MSL_ST2_LIFE, A.MSL_I32, s, s, 1, 16)
+            d, rate = A.autotune_stencil2d(A.MSL_ST2_LIFE, A.MSL_I32, s, s, 1, 64)
             self.tuned["life_temporal_depth"] = d
             p = self.parts["life"]
             p.launches = (self.life_steps + d - 1) // d

@@ -221,8 +221,17 @@ int msl_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, int c
     if (depth > 1 && stencil2d_tb_smem<double>(radius, depth) > kMaxStencilSmem)
         return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_stencil2d_iterate: temporal depth %d too deep for radius %d",
                         depth, radius);
+    // Life: every launch after the first reads the output of a Life launch,
+    // whose cells are all 0 or 1, and may take the packed kernel.
+    const bool life_packed = dtype == MSL_I32 && kind == MSL_ST2_LIFE && radius == 1 && neutral == 0.0;
+    int launch_no = 0;
     return iterate("msl_stencil2d_iterate", a, b, iters, depth, residual, result_in_b,
                    [&](void *p, void *q, int k, const Sweep &sw) {
+                       const bool binary_in = launch_no++ > 0;
+                       if (life_packed && binary_in && !sw.resid && sw.tma) {
+                           cudaError_t e = life_packed_2d(p, q, rows, cols, k);
+                           if (e != cudaErrorNotSupported) return e;
+                       }
                        if (k > 1) return tb_sweeps_2d(dtype, kind, p, q, rows, cols, radius, k, neutral, sw.resid, sw.tma);
                        return dispatch2d(dtype, kind, p, q, rows, cols, radius, neutral, sw);
                    });

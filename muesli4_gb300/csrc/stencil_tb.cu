@@ -1,5 +1,6 @@
 // Temporally blocked 2-D sweeps (several sweeps per launch) for the built-in
 // Jacobi, heat2D and Life functors; see stencil2d_tb_kernel.
+#include "../include/detail/msl_life.cuh"
 #include "stencil_functors.cuh"
 
 namespace msl {
@@ -38,6 +39,11 @@ cudaError_t tb_sweeps_2d(int dtype, int kind, const void *in, void *out, int row
                                                 (int32_t)(long long)neutral, StLife{}, resid, c.err_word, c.stream, tma);
     }
     return cudaErrorInvalidValue;
+}
+
+cudaError_t life_packed_2d(const void *in, void *out, int rows, int cols, int depth) {
+    auto &c = rt::ctx();
+    return launch_life_packed((const int32_t *)in, (int32_t *)out, rows, cols, depth, c.err_word, c.stream);
 }
 
 }  // namespace builtin
