@@ -822,6 +822,8 @@ def main():
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[0.25, 0.5, 1.0, 2.0])
     ap.add_argument("--temporal-depth", type=int, default=0,
                     help="sweeps per launch of the iterated 2-D stencils (0: the autotuner's choice)")
+    ap.add_argument("--stencil3d-depth", type=int, default=1, choices=[1, 2],
+                    help="heat3D sweeps per launch: 1 one sweep (default), 2 the z-marching kernel")
     ap.add_argument("--stencil3d-persistent", type=int, default=-1, choices=[-1, 0, 1],
                     help="3-D stencil kernel: 1 persistent, 0 one CTA per block, -1 library default")
     args = ap.parse_args()
@@ -845,6 +847,7 @@ def main():
     from muesli4_gb300 import abi as A
     A.init(dist.local_rank)
     A.set_stencil3d_persistent(args.stencil3d_persistent)
+    A.set_stencil3d_depth(args.stencil3d_depth)
     w = WORKLOADS[args.workload](A)
     w.setup()
     if args.temporal_depth > 0:  # after setup: overrides the autotuner's record

@@ -61,7 +61,7 @@ def load() -> ctypes.CDLL:
         "msl_init": [i], "msl_terminate": [], "msl_sync": [], "msl_get_stream": [ctypes.POINTER(vp)],
         "msl_set_stream": [vp], "msl_device_info": [ip, ctypes.POINTER(sz), ctypes.POINTER(sz)],
         "msl_launch_count": [ctypes.POINTER(ctypes.c_ulonglong)], "msl_set_tma": [i],
-        "msl_set_stencil3d_persistent": [i],
+        "msl_set_stencil3d_persistent": [i], "msl_set_stencil3d_depth": [i],
         "msl_alloc": [ctypes.POINTER(vp), sz], "msl_free": [vp], "msl_upload": [vp, vp, sz],
         "msl_download": [vp, vp, sz], "msl_copy": [vp, vp, sz], "msl_fill": [i, vp, sz, d],
         "msl_map": [i, i, vp, vp, sz, dp], "msl_zip": [i, i, vp, vp, vp, sz], "msl_zip3": [i, i, vp, vp, vp, vp, sz],
@@ -140,6 +140,11 @@ def set_tma(enabled: bool) -> None:
 def set_stencil3d_persistent(mode: int) -> None:
     """3-D stencil kernel: 1 persistent, 0 one CTA per block, -1 default."""
     check(load().msl_set_stencil3d_persistent(int(mode)), "msl_set_stencil3d_persistent")
+
+
+def set_stencil3d_depth(sweeps: int) -> None:
+    """heat3D sweeps per launch: 1 one sweep (default), 2 the z-marching kernel."""
+    check(load().msl_set_stencil3d_depth(int(sweeps)), "msl_set_stencil3d_depth")
 
 
 def set_temporal_depth(depth: int) -> None:

@@ -5,6 +5,9 @@
 // Reference: DM::mapStencil (src/dm.cpp:1535-1591) and DC::mapStencil
 // (src/dc.cpp:559-592); functors examples/heatdiffusion.cpp:55-76,
 // examples/gameoflife.cpp:22-42, examples/meanblur2.cpp:46-57.
+#include <cmath>
+
+#include "../include/detail/msl_stencil3d_tb.cuh"
 #include "stencil_functors.cuh"
 
 using namespace msl;
@@ -23,6 +26,11 @@ struct Sweep {
 
 // 3-D kernel choice of msl_set_stencil3d_persistent (-1 = default).
 std::atomic<int> g_persistent3d{-1};
+// Sweeps per launch of msl_stencil3d_iterate where the z-marching kernel
+// applies (1 or 2). One sweep per launch is the default: on heat3D 512^3 the
+// one-sweep kernel runs at the HBM roofline (786 GCUPS) while the z-marching
+// kernel, with half the HBM traffic, is bound by instruction issue (651).
+std::atomic<int> g_depth3d{1};
 
 template <typename S>
 cudaError_t sweep2d(int kind, const S *in, S *out, int rows, int cols, int r, double neutral_d, const Sweep &sw) {
@@ -189,6 +197,12 @@ int msl_set_tma(int enabled) {
     return MSL_OK;
 }
 
+int msl_set_stencil3d_depth(int sweeps) {
+    if (sweeps < 1 || sweeps > 2) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_set_stencil3d_depth: %d not 1 or 2", sweeps);
+    g_depth3d.store(sweeps);
+    return MSL_OK;
+}
+
 int msl_set_stencil3d_persistent(int mode) {
     if (mode < -1 || mode > 1) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_set_stencil3d_persistent: %d not in -1..1", mode);
     g_persistent3d.store(mode);
@@ -254,8 +268,17 @@ int msl_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int 
     if (int e = rt::require_init()) return e;
     if (int e = check3d("msl_stencil3d_iterate", dtype, kind, a, b, depth, rows, cols, radius)) return e;
     if (iters < 1) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_stencil3d_iterate: iters must be >= 1");
-    return iterate("msl_stencil3d_iterate", a, b, iters, 1, residual, result_in_b,
-                   [&](void *p, void *q, int, const Sweep &sw) {
+    // heat3D (FP32, radius 1, neutral +0) on grids TMA can address: two
+    // sweeps per launch by z-marching
+    const bool ztb = dtype == MSL_F32 && kind == MSL_ST3_HEAT7 && radius == 1 && neutral == 0.0 &&
+                     !std::signbit(neutral) && g_depth3d.load(std::memory_order_relaxed) == 2 && tma_enabled() &&
+                     stencil_tma_ok<float>(a, cols, kZtbPitch, kZtbRows) &&
+                     stencil_tma_ok<float>(b, cols, kZtbPitch, kZtbRows);
+    return iterate("msl_stencil3d_iterate", a, b, iters, ztb ? 2 : 1, residual, result_in_b,
+                   [&](void *p, void *q, int k, const Sweep &sw) {
+                       if (k == 2)
+                           return launch_stencil3d_ztb((const float *)p, (float *)q, depth, rows, cols,
+                                                       StHeat7<float>{}, sw.resid, ctx().err_word, ctx().stream);
                        return dispatch3d(dtype, kind, p, q, depth, rows, cols, radius, neutral, sw);
                    });
 }

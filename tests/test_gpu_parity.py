@@ -338,6 +338,26 @@ def test_stencil3d_heat(gpu, shape, kernel):
         gpu.set_stencil3d_persistent(-1)
 
 
+@pytest.mark.parametrize("sweeps_per_launch", [2, 1])
+@pytest.mark.parametrize("shape", [(1, 1, 4), (5, 7, 11), (33, 17, 70), (40, 64, 64), (70, 20, 36), (65, 33, 200)],
+                         ids=str)
+def test_stencil3d_heat_z_marching(gpu, shape, sweeps_per_launch):
+    """heat3D two sweeps per launch (z-marching kernel) against the oracle for
+    1..5 sweeps (odd counts end with a one-sweep launch), with the residual of
+    the last sweep; chunk, block and grid edges fall inside the shapes."""
+    x = W.heat_cube(*shape, seed=sum(shape) + 1)
+    gpu.set_stencil3d_depth(sweeps_per_launch)
+    try:
+        for iters in range(1, 6):
+            a, b = dev(gpu, x), gpu.DeviceArray(x.shape, x.dtype)
+            last, res = gpu.stencil3d_iterate(gpu.MSL_ST3_HEAT7, a, b, 1, 0.0, iters)
+            want, _, want_res = O.stencil3d_iterate(gpu.MSL_ST3_HEAT7, x, 1, 0.0, iters)
+            assert bits_equal(last.download(), want), iters
+            assert res == want_res, iters
+    finally:
+        gpu.set_stencil3d_depth(1)
+
+
 @pytest.mark.parametrize("persistent", [0, 1])
 @pytest.mark.parametrize("r", [1, 2, 3])
 @pytest.mark.parametrize("shape", [(9, 10, 11), (24, 20, 68)], ids=str)
