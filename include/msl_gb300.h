@@ -123,6 +123,14 @@ int msl_free(void *dptr);
 int msl_upload(void *dst_device, const void *src_host, size_t bytes);
 /* Device -> host: DS::updateHost / gather (src/ds.cpp:465-484, 539-591). Synchronous. */
 int msl_download(void *dst_host, const void *src_device, size_t bytes);
+/* Stream-ordered forms of msl_upload / msl_download: enqueued on `stream` (a
+ * cudaStream_t; NULL = the library stream) without waiting, so a transfer can
+ * overlap kernels on other buffers. The caller orders them against its other
+ * work with events and keeps the host buffer (pinned, for an asynchronous
+ * copy) alive until the copy has finished. The reference copies synchronously
+ * in updateDevice / updateHost (src/ds.cpp:442-484). */
+int msl_upload_async(void *dst_device, const void *src_host, size_t bytes, void *stream);
+int msl_download_async(void *dst_host, const void *src_device, size_t bytes, void *stream);
 /* Device -> device copy kernel: copyKernel (src/copy_kernel.cu:33-43), gather(DS&) (src/ds.cpp:562-581). */
 int msl_copy(void *dst_device, const void *src_device, size_t bytes);
 /* DS::fill(const T&) (src/ds.cpp:290-305). */

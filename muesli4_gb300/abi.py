@@ -64,6 +64,7 @@ def load() -> ctypes.CDLL:
         "msl_set_stencil3d_persistent": [i], "msl_set_stencil3d_depth": [i],
         "msl_alloc": [ctypes.POINTER(vp), sz], "msl_free": [vp], "msl_upload": [vp, vp, sz],
         "msl_download": [vp, vp, sz], "msl_copy": [vp, vp, sz], "msl_fill": [i, vp, sz, d],
+        "msl_upload_async": [vp, vp, sz, vp], "msl_download_async": [vp, vp, sz, vp],
         "msl_map": [i, i, vp, vp, sz, dp], "msl_zip": [i, i, vp, vp, vp, sz], "msl_zip3": [i, i, vp, vp, vp, vp, sz],
         "msl_map_index": [i, i, vp, vp, i, llp, dp], "msl_zip_index": [i, i, vp, vp, vp, i, llp, dp],
         "msl_fold": [i, i, vp, sz, vp], "msl_fold_absdiff_max": [i, vp, vp, sz, dp],

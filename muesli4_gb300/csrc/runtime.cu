@@ -250,6 +250,33 @@ int msl_download(void *dst, const void *src, size_t bytes) {
     return MSL_OK;
 }
 
+// Stream-ordered transfers: enqueued on `stream` (a cudaStream_t; NULL = the
+// library stream) without waiting, so copies of one buffer can overlap
+// kernels working on another. The caller orders them against its other work
+// (events) and keeps the host buffer alive and unchanged until the copy is
+// done; with pinned host memory the copy engines run them asynchronously.
+int msl_upload_async(void *dst, const void *src, size_t bytes, void *stream) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    if (int e = rt::require_init()) return e;
+    if (bytes == 0) return MSL_OK;
+    if (!dst || !src) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_upload_async: NULL pointer");
+    MSL_TRY_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream ? (cudaStream_t)stream : c.stream),
+                 "msl_upload_async");
+    return MSL_OK;
+}
+
+int msl_download_async(void *dst, const void *src, size_t bytes, void *stream) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    if (int e = rt::require_init()) return e;
+    if (bytes == 0) return MSL_OK;
+    if (!dst || !src) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_download_async: NULL pointer");
+    MSL_TRY_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream ? (cudaStream_t)stream : c.stream),
+                 "msl_download_async");
+    return MSL_OK;
+}
+
 int msl_copy(void *dst, const void *src, size_t bytes) {
     auto &c = ctx();
     std::lock_guard<std::recursive_mutex> g(c.mu);

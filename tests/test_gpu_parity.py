@@ -372,3 +372,23 @@ def test_stencil3d_box(gpu, r, shape, persistent):
                 assert bits_equal(o.download(), O.stencil3d(kind, x, r, neutral)), (kind, r, neutral)
     finally:
         gpu.set_stencil3d_persistent(-1)
+
+
+def test_async_transfers_round_trip(gpu):
+    """msl_upload_async / msl_download_async: stream-ordered copies between
+    pinned host memory and the device, on a caller's stream and on the
+    library stream (NULL)."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    x = np.random.default_rng(3).random(1 << 20, dtype=np.float32)
+    src = torch.from_numpy(x.copy()).pin_memory()
+    dst = torch.empty_like(src).pin_memory()
+    d = gpu.DeviceArray((x.size,), np.float32)
+    side = torch.cuda.Stream()
+    L = gpu.load()
+    gpu.check(L.msl_upload_async(d.ptr, ctypes.c_void_p(src.data_ptr()), x.nbytes, ctypes.c_void_p(side.cuda_stream)),
+              "msl_upload_async")
+    side.synchronize()
+    gpu.check(L.msl_download_async(ctypes.c_void_p(dst.data_ptr()), d.ptr, x.nbytes, None), "msl_download_async")
+    gpu.sync()
+    assert np.array_equal(dst.numpy(), x)
