@@ -185,6 +185,9 @@ class Part:
     def __init__(self, name, updates, launches, bytes_per_launch, dtype):
         self.name, self.updates, self.launches = name, updates, launches
         self.bytes_per_launch, self.dtype = bytes_per_launch, dtype
+        # one read and one write of the grid: what a launch that runs several
+        # sweeps (temporal blocking) must move at least
+        self.compulsory_bytes = bytes_per_launch
         self.ms = 0.0
 
 
@@ -204,6 +207,7 @@ class StencilSuite:
             self.parts["box"] = Part("box_mean_r1-10", n2 * len(BOX_RADII), len(BOX_RADII), 8 * n2, "f32")
         if "life" in parts:
             self.parts["life"] = Part("life", n2 * life_steps, life_steps, 8 * n2, "i32")
+            self.parts["life"].compulsory_bytes = 8 * n2
         if "heat" in parts:
             self.parts["heat"] = Part("heat3d", n3 * heat_steps, heat_steps, 8 * n3, "f32")
 
@@ -253,7 +257,7 @@ class StencilSuite:
             d, rate = A.autotune_stencil2d(A.MSL_ST2_LIFE, A.MSL_I32, s, s, 1, 64)
             self.tuned["life_temporal_depth"] = d
             p = self.parts["life"]
-            p.launches = (self.life_steps + d - 1) // d
+            p.launches = life_launches(self.life_steps, d)
             p.bytes_per_launch = 8 * s * s * self.life_steps // p.launches  # algorithmic, averaged over launches
 
     def updates(self):
@@ -393,6 +397,7 @@ class Jacobi:
         p = self.parts["jacobi"]
         p.launches = (self.iters + d - 1) // d
         p.bytes_per_launch = 8 * self.side * self.side * self.iters // p.launches
+        p.compulsory_bytes = 8 * self.side * self.side
 
     def updates(self):
         return self.parts["jacobi"].updates
@@ -825,6 +830,12 @@ def run_batch(args, dist: Dist):
         print(json.dumps(line), flush=True)
 
 
+def life_launches(steps, depth):
+    """Launches of a Life iteration on a width that is a multiple of 4: one
+    generation cell by cell, then `depth` packed generations per launch."""
+    return 1 + (steps - 1 + depth - 1) // depth
+
+
 DRAM_TRAFFIC_PER_LAUNCH = {
     "heat3d": 1027.49e6,         # profiles/heat7_stencil3d_512.md (one sweep of 512^3)
     "life": 495.25e6,            # profiles/life8_stencil2d_8192.md (two sweeps of 8192^2)
@@ -880,7 +891,7 @@ def main():
         if hasattr(w, "tuned") and "life_temporal_depth" in w.tuned:
             w.tuned["life_temporal_depth"] = args.temporal_depth
             p = w.parts["life"]
-            p.launches = (w.life_steps + args.temporal_depth - 1) // args.temporal_depth
+            p.launches = life_launches(w.life_steps, args.temporal_depth)
             p.bytes_per_launch = 8 * w.side ** 2 * w.life_steps // p.launches
     ev = Events(A)
     for _ in range(args.warmup):
@@ -951,8 +962,8 @@ def main():
     # DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum +
     # dram__bytes_write.sum) from the ncu captures summarised in profiles/.
     traffic = DRAM_TRAFFIC_PER_LAUNCH.get(p.name)
-    if p.name == "life" and getattr(w, "tuned", {}).get("life_temporal_depth") != 2:
-        traffic = None  # captured at temporal depth 2
+    if p.name == "life" and getattr(w, "tuned", {}).get("life_temporal_depth") != 8:
+        traffic = None  # captured at temporal depth 8
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
@@ -974,7 +985,10 @@ def main():
             "e2e": {"value": e2e_value, "unit": w.unit, "h2d_bytes_per_step": w.h2d, "d2h_bytes_per_step": w.d2h},
             "roofline": {"bound": "hbm", "kernel": p.name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                         "bytes_per_launch": p.bytes_per_launch},
+                         "bytes_per_launch": p.bytes_per_launch,
+                         # several sweeps per launch: the grid's one read and write per launch
+                         "compulsory_bytes_per_launch": p.compulsory_bytes,
+                         "compulsory_frac": p.compulsory_bytes / avg_launch_s / 1e9 / peak},
             "parts": parts_out,
             "cpu_baseline": cpu,
             "gpu_launches": launches,

@@ -347,7 +347,7 @@ int msl_server_stop(void *server);
 
 /* ---- autotuner -------------------------------------------------------------
  * Times msl_stencil2d_iterate over `iters` sweeps of a rows x cols grid for
- * every temporal depth that fits (1, 2, 3, 4, 6, 8), on scratch grids it
+ * every temporal depth that fits (1, 2, 3, 4, 6, 8, 12, 16), on scratch grids it
  * allocates and frees, records the fastest for (dtype, kind, radius, grid-size
  * class) and returns it with its rate in cell updates per second. The record
  * is used by later iterate calls when the temporal depth is 0. No reference

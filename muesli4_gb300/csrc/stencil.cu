@@ -150,16 +150,17 @@ std::atomic<int> g_tma_enabled{1};
 bool tma_enabled() { return g_tma_enabled.load(std::memory_order_relaxed) != 0; }
 
 // `iters` ping-pong sweeps a -> b -> a ..., `depth` sweeps per launch (the
-// last launch takes the remainder). The residual is fused into the last sweep.
+// first launch runs `first` sweeps when that is > 0; the last launch takes the
+// remainder). The residual is fused into the last sweep.
 template <class Launch>
 int iterate(const char *what, void *a, void *b, int iters, int depth, double *residual, int *result_in_b,
-            Launch launch) {
+            Launch launch, int first = 0) {
     auto &c = ctx();
     Sweep sw{nullptr, tma_enabled()};
     if (residual) MSL_TRY_CUDA(cudaMemsetAsync(c.resid, 0, sizeof(unsigned long long), c.stream), what);
     void *p = a, *q = b;
     for (int i = 0; i < iters;) {
-        const int k = std::min(std::max(depth, 1), iters - i);
+        const int k = std::min(std::max(i == 0 && first > 0 ? first : depth, 1), iters - i);
         sw.resid = (residual && i + k == iters) ? c.resid : nullptr;
         cudaError_t e = launch(p, q, k, sw);
         if (e != cudaSuccess) return rt::cuda_fail(e, what);
@@ -238,17 +239,21 @@ int msl_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, int c
     // Life: every launch after the first reads the output of a Life launch,
     // whose cells are all 0 or 1, and may take the packed kernel.
     const bool life_packed = dtype == MSL_I32 && kind == MSL_ST2_LIFE && radius == 1 && neutral == 0.0;
+    // The first launch then runs a single generation (the cell-by-cell kernel
+    // at full memory speed) and every later one `depth` packed generations.
+    const int first = life_packed && cols % 4 == 0 ? 1 : 0;
     int launch_no = 0;
     return iterate("msl_stencil2d_iterate", a, b, iters, depth, residual, result_in_b,
                    [&](void *p, void *q, int k, const Sweep &sw) {
                        const bool binary_in = launch_no++ > 0;
-                       if (life_packed && binary_in && !sw.resid && sw.tma) {
+                       if (life_packed && binary_in && !sw.resid) {
                            cudaError_t e = life_packed_2d(p, q, rows, cols, k);
                            if (e != cudaErrorNotSupported) return e;
                        }
                        if (k > 1) return tb_sweeps_2d(dtype, kind, p, q, rows, cols, radius, k, neutral, sw.resid, sw.tma);
                        return dispatch2d(dtype, kind, p, q, rows, cols, radius, neutral, sw);
-                   });
+                   },
+                   first);
 }
 
 int msl_stencil3d(int dtype, int kind, const void *in, void *out, int depth, int rows, int cols, int radius,

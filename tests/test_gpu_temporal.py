@@ -50,9 +50,12 @@ def test_heat2d_fused_with_neutral(gpu, depth, d):
     assert res == want_res
 
 
-@pytest.mark.parametrize("d", [2, 4, 8])
-@pytest.mark.parametrize("shape", [(64, 80), (1000, 1024)], ids=str)
+@pytest.mark.parametrize("d", [1, 2, 3, 4, 5, 6, 7, 8, 9, 12, 16])
+@pytest.mark.parametrize("shape", [(64, 80), (1000, 1024), (300, 1028), (130, 998), (7, 4)], ids=str)
 def test_life_fused(gpu, depth, d, shape):
+    """Every launch after the first runs the packed kernel where the width
+    allows it (cols a multiple of 4), the cell-by-cell kernels otherwise; the
+    iteration count leaves a remainder launch of 3 generations."""
     depth(d)
     board = W.life_board(*shape, seed=d)
     a, b = gpu.DeviceArray.from_host(board), gpu.DeviceArray(board.shape, np.int32)
