@@ -254,7 +254,9 @@ class StencilSuite:
         # iterated 2-D part; its records are used by the timed iterate calls.
         self.tuned = {}
         if "life" in self.parts:
-            d, rate = A.autotune_stencil2d(A.MSL_ST2_LIFE, A.MSL_I32, s, s, 1, 64)
+            d = getattr(self, "fixed_depth", 0)
+            if d <= 0:
+                d, rate = A.autotune_stencil2d(A.MSL_ST2_LIFE, A.MSL_I32, s, s, 1, 64)
             self.tuned["life_temporal_depth"] = d
             p = self.parts["life"]
             p.launches = life_launches(self.life_steps, d)
@@ -392,7 +394,9 @@ class Jacobi:
         self.dev = {"jacobi": [A.DeviceArray.from_host(g), A.DeviceArray(g.shape, np.float32)]}
         self.h2d, self.d2h = h.nbytes, h.nbytes + 8
         self.residual = None
-        d, _ = A.autotune_stencil2d(A.MSL_ST2_JACOBI5, A.MSL_F32, self.side, self.side, 1, 64)
+        d = getattr(self, "fixed_depth", 0)
+        if d <= 0:
+            d, _ = A.autotune_stencil2d(A.MSL_ST2_JACOBI5, A.MSL_F32, self.side, self.side, 1, 64)
         self.tuned = {"temporal_depth": d}
         p = self.parts["jacobi"]
         p.launches = (self.iters + d - 1) // d
@@ -885,14 +889,10 @@ def main():
     A.set_stencil3d_persistent(args.stencil3d_persistent)
     A.set_stencil3d_depth(args.stencil3d_depth)
     w = WORKLOADS[args.workload](A)
+    w.fixed_depth = args.temporal_depth  # > 0: no autotuning of the Life depth
     w.setup()
     if args.temporal_depth > 0:  # after setup: overrides the autotuner's record
         A.set_temporal_depth(args.temporal_depth)
-        if hasattr(w, "tuned") and "life_temporal_depth" in w.tuned:
-            w.tuned["life_temporal_depth"] = args.temporal_depth
-            p = w.parts["life"]
-            p.launches = life_launches(w.life_steps, args.temporal_depth)
-            p.bytes_per_launch = 8 * w.side ** 2 * w.life_steps // p.launches
     ev = Events(A)
     for _ in range(args.warmup):
         w.step()

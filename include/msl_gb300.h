@@ -245,8 +245,11 @@ int msl_set_stencil3d_depth(int sweeps);
 /* Sweeps fused into one launch by msl_stencil2d_iterate (temporal blocking:
  * the CTA runs depth-1 sweeps on a shared-memory tile with a depth*r halo and
  * writes the last; results are identical to single sweeps). 0 (default) uses
- * the autotuner's choice for the grid, or 1 when none was recorded. Applies to
- * Jacobi, heat2D (F32, F64, BF16) and Life. No reference counterpart. */
+ * the autotuner's choice for the grid, or 1 when none was recorded; at most
+ * 32. Applies to Jacobi, heat2D (F32, F64, BF16) and Life. An int32 Life
+ * iteration with neutral 0 runs its first generation cell by cell and then
+ * `depth` generations per launch on cells packed one bit each (its cells are
+ * then all 0 or 1), with identical results. No reference counterpart. */
 int msl_set_temporal_depth(int depth);
 /* out = f(view, x, y) for every cell of a rows x cols grid; `radius` is the
  * stencil size r, `neutral` the value outside the grid. in != out.
@@ -347,7 +350,7 @@ int msl_server_stop(void *server);
 
 /* ---- autotuner -------------------------------------------------------------
  * Times msl_stencil2d_iterate over `iters` sweeps of a rows x cols grid for
- * every temporal depth that fits (1, 2, 3, 4, 6, 8, 12, 16), on scratch grids it
+ * every temporal depth that fits (1, 2, 3, 4, 6, 8, 12, 16, 24, 32), on scratch grids it
  * allocates and frees, records the fastest for (dtype, kind, radius, grid-size
  * class) and returns it with its rate in cell updates per second. The record
  * is used by later iterate calls when the temporal depth is 0. No reference

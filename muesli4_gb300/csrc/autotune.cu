@@ -91,7 +91,7 @@ int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, 
     double best_r = 0.0;
     int rc = MSL_OK;
     const int saved = 0;
-    const int candidates[] = {1, 2, 3, 4, 6, 8, 12, 16};
+    const int candidates[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32};
     const int ncand = (int)(sizeof candidates / sizeof candidates[0]);
     double rate[ncand] = {};
     bool usable[ncand] = {};

@@ -211,7 +211,7 @@ int msl_set_stencil3d_persistent(int mode) {
 }
 
 int msl_set_temporal_depth(int depth) {
-    if (depth < 0 || depth > 16) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_set_temporal_depth: %d not in 0..16", depth);
+    if (depth < 0 || depth > 32) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_set_temporal_depth: %d not in 0..32", depth);
     g_temporal_depth.store(depth);
     return MSL_OK;
 }
@@ -233,15 +233,18 @@ int msl_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, int c
     if (int e = check2d("msl_stencil2d_iterate", dtype, kind, a, b, rows, cols, radius)) return e;
     if (iters < 1) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_stencil2d_iterate: iters must be >= 1");
     const int depth = depth_for(dtype, kind, rows, cols, radius);
-    if (depth > 1 && stencil2d_tb_smem<double>(radius, depth) > kMaxStencilSmem)
+    // Life: every launch after the first reads the output of a Life launch,
+    // whose cells are all 0 or 1, and may take the bit-packed kernel. The first
+    // launch then runs a single generation (the cell-by-cell kernel at full
+    // memory speed) and every later one `depth` packed generations; only a
+    // last launch with a residual runs several generations cell by cell.
+    const bool life_packed = dtype == MSL_I32 && kind == MSL_ST2_LIFE && radius == 1 && neutral == 0.0 &&
+                             depth <= builtin::kLifePackedMaxDepth;
+    const int first = life_packed ? 1 : 0;
+    const bool generic_tb = depth > 1 && (!life_packed || residual);
+    if (generic_tb && stencil2d_tb_smem<double>(radius, depth) > kMaxStencilSmem)
         return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_stencil2d_iterate: temporal depth %d too deep for radius %d",
                         depth, radius);
-    // Life: every launch after the first reads the output of a Life launch,
-    // whose cells are all 0 or 1, and may take the packed kernel.
-    const bool life_packed = dtype == MSL_I32 && kind == MSL_ST2_LIFE && radius == 1 && neutral == 0.0;
-    // The first launch then runs a single generation (the cell-by-cell kernel
-    // at full memory speed) and every later one `depth` packed generations.
-    const int first = life_packed && cols % 4 == 0 ? 1 : 0;
     int launch_no = 0;
     return iterate("msl_stencil2d_iterate", a, b, iters, depth, residual, result_in_b,
                    [&](void *p, void *q, int k, const Sweep &sw) {

@@ -174,6 +174,7 @@ bool tb_supported_2d(int dtype, int kind);
 // `depth` Life generations of an int32 grid whose cells are all 0 or 1, with
 // the dead (0) border, on the packed kernel of msl_life.cuh (stencil_tb.cu);
 // cudaErrorNotSupported when the grid does not suit it.
+constexpr int kLifePackedMaxDepth = 32;  // generations per launch of life_packed_2d
 cudaError_t life_packed_2d(const void *in, void *out, int rows, int cols, int depth);
 }  // namespace builtin
 }  // namespace msl

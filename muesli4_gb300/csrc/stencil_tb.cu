@@ -41,6 +41,8 @@ cudaError_t tb_sweeps_2d(int dtype, int kind, const void *in, void *out, int row
     return cudaErrorInvalidValue;
 }
 
+static_assert(kLifePackedMaxDepth == gpu::kLifeMaxDepth, "Life kernel depth limit");
+
 cudaError_t life_packed_2d(const void *in, void *out, int rows, int cols, int depth) {
     auto &c = rt::ctx();
     return launch_life_packed((const int32_t *)in, (int32_t *)out, rows, cols, depth, c.stream);

@@ -1,36 +1,36 @@
 // Game of Life on a grid whose cells are all 0 or 1, several generations per
-// launch, four cells packed into each 32-bit word of shared memory.
+// launch, one bit per cell in shared memory (32 cells per word).
 //
 // The reference's rule (examples/gameoflife.cpp:22-42) on int32 cells: a cell
 // becomes 1 when alive == 1 and its eight neighbours sum to 2 or 3, or when
 // alive == 0 and they sum to 3; otherwise 0. Every output of the rule is 0 or
 // 1, so from the second generation of an iteration on, every input is too.
-// For 0/1 cells the rule is `(sum | alive) == 3`, and sums of up to nine 0/1
-// cells fit in a byte: with one cell per byte, ordinary 32-bit additions add
-// four cells at once (no byte ever carries), `__byte_perm` forms the words of
-// the left and right neighbours, and a per-byte zero test evaluates the rule
-// for four cells -- about four integer instructions per cell update instead of
-// eight neighbour loads and additions. Results are identical to the
-// cell-by-cell functor for 0/1 inputs, which the caller guarantees (this
-// kernel is used only on the outputs of Life sweeps).
+// For 0/1 cells the neighbour count fits in bit-sliced adders: with bit i of a
+// word holding cell 32w + i, the words of left and right neighbours are
+// funnel shifts of the row's words, full adders (XOR3 and majority, one
+// three-input logic instruction each) sum a row's three cells, and the count
+// bits c0, c1, c2 (mod 8; a count of 8 reads as 0, which the rule treats like
+// 8) give the rule as `c1 & ~c2 & (c0 | alive)` -- about 20 instructions per
+// 32 cell updates. Results are identical to the cell-by-cell functor for 0/1
+// inputs, which the caller guarantees (this kernel is used only on the
+// outputs of Life sweeps).
 //
-// One CTA computes a 128 x 64 block D generations ahead. It reads the block
-// and its halo with coalesced 16-byte loads (zeros outside the grid), packs
-// the cells into bytes as it stores them to shared memory, runs the
-// generations between two packed buffers and writes the last one as int32.
-// Cells outside the grid are kept at 0 after every generation, as the dead
-// border of the reference's neutral value 0. D is a template parameter, so
-// every loop bound and index division is a compile-time constant.
+// One CTA computes a 960 x 64 block `depth` generations ahead (depth <= 32).
+// Its window is 32 words (1024 cells) wide -- one word per lane, one word of
+// halo either side -- and 64 + 2 depth rows high. Staging: each warp reads
+// whole window rows with coalesced 4-byte loads (zeros outside the grid) and
+// packs 32 cells into a word with one ballot. Generations ping-pong between
+// two bit buffers; a warp computes a strip of 8 rows for all 32 words of the
+// window (lane = word), reusing each row's three-cell sums for the rows above
+// and below it. Cells outside the grid are kept at 0 after every generation,
+// as the dead border of the reference's neutral value 0.
 //
 // Rows: generation s is computed on rows [s, TH - s), exactly the rows the
-// next one reads, so a D-row halo suffices. Columns: each generation computes
-// the window's words 1 .. NW-2 only. The edge words of the second buffer are
-// zeroed once and those of the first keep the staged cells, so every word
-// read holds 0/1 bytes (no byte of a sum can carry into its neighbour); the
-// edge words are stale after the first generation, and every generation after
-// it spreads that one cell further in (cells < s + 3 from a window edge are
-// wrong after generation s). The column halo is therefore D + 3 cells,
-// rounded up to whole words.
+// next one reads, so a depth-row halo suffices. Columns: the words beyond the
+// window are zero pads, so the window's outermost cells see dead neighbours
+// there; the error spreads one cell per generation, so after `depth`
+// generations cells < depth from a window edge may be wrong and the block,
+// one word (32 cells) in from either edge, is exact for depth <= 32.
 #pragma once
 
 #include "msl_stencil.cuh"
@@ -38,168 +38,142 @@
 namespace msl {
 namespace gpu {
 
-constexpr int kLifeBX = 128, kLifeBY = 64;  // output block, cells
-constexpr int kLifeThreads = 256;
-constexpr int kLifeStrip = 6;      // word rows per thread task (vertical reuse of the row sums)
-constexpr int kLifeMaxDepth = 16;  // generations per launch handled by this kernel
+constexpr int kLifeWords = 32;                  // words per window row, one per lane
+constexpr int kLifePitch = kLifeWords + 2;      // plus a zero pad either side
+constexpr int kLifeBW = kLifeWords - 2;         // words per block row
+constexpr int kLifeBX = kLifeBW * 32;           // 960 cells
+constexpr int kLifeBY = 64;                     // block rows
+constexpr int kLifeWarps = 8, kLifeThreads = 32 * kLifeWarps;
+constexpr int kLifeStrip = 8;                   // rows per warp task (vertical reuse of the row sums)
+constexpr int kLifeMaxDepth = 32;               // generations per launch (the block's column halo)
+constexpr int kLifeLoadBatch = 8;               // loads in flight per lane while staging
 
-template <int D>
-struct LifeWindow {
-    static constexpr int kHX = (D + 3 + 3) / 4 * 4;  // column halo, cells (whole words)
-    static constexpr int kP = kLifeBX + 2 * kHX;     // window width, cells
-    static constexpr int kNW = kP / 4;               // words per window row
-    static constexpr int kTH = kLifeBY + 2 * D;      // window height, rows
-    static constexpr int kWords = kNW * kTH;
-    static_assert(kHX >= D + 3 && kHX % 4 == 0, "column halo");
-};
-
-// Bytes equal to 3 -> 1, others -> 0, for bytes <= 15 (a per-byte zero test
-// of x ^ 3: adding 0x7F to a byte <= 15 sets its top bit exactly when it is
-// not 0 and never carries into the next byte).
-MSL_DEV uint32_t life_rule4(uint32_t sum, uint32_t alive) {
-    const uint32_t u = ((sum | alive) ^ 0x03030303u) + 0x7F7F7F7Fu;
-    return (~u >> 7) & 0x01010101u;
+inline size_t life_bits_smem(int depth) {
+    return 2 * (size_t)(kLifeBY + 2 * depth) * kLifePitch * sizeof(uint32_t);
 }
 
-// Row sums of three horizontally adjacent cells for the four cells of word
-// `c`, given the words to its left and right.
-MSL_DEV uint32_t life_hsum(uint32_t l, uint32_t c, uint32_t r) {
-    return __byte_perm(l, c, 0x6543) + c + __byte_perm(c, r, 0x4321);
-}
+MSL_DEV uint32_t xor3(uint32_t a, uint32_t b, uint32_t c) { return a ^ b ^ c; }
+MSL_DEV uint32_t maj3(uint32_t a, uint32_t b, uint32_t c) { return (a & b) | (c & (a | b)); }
 
-// Bytes of word `w` (cells wx0 + 4w .. + 3) that lie in [0, cols): the word
-// is wholly inside or outside, since wx0 and cols are multiples of 4.
-MSL_DEV uint32_t life_colmask(int wx0, int w, int cols) {
-    const int gx = wx0 + 4 * w;
-    return (gx >= 0 && gx < cols) ? 0xFFFFFFFFu : 0u;
-}
-
-// Generation s: dst = rule(src) on rows [s, TH - s), words 1 .. NW-2.
-// MASK (blocks whose window leaves the grid) clears the cells outside it.
-template <int D, bool MASK>
-MSL_DEV void life_generation(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, int s, int wx0, int cols,
-                             int row_lo, int row_hi) {
-    using Wd = LifeWindow<D>;
-    constexpr int ncw = Wd::kNW - 2;
-    const int nrows = Wd::kTH - 2 * s, ns = (nrows + kLifeStrip - 1) / kLifeStrip;
-    for (int t = threadIdx.x; t < ncw * ns; t += kLifeThreads) {
-        const int sidx = t / ncw, w = 1 + (t - sidx * ncw);
-        const int r0 = s + min(sidx * kLifeStrip, nrows - kLifeStrip);  // the last strip ends at the last row
-        uint32_t h[kLifeStrip + 2], c[kLifeStrip + 2];
+// One warp, one strip: rows [r0, r0 + kLifeStrip) of every window word
+// (lane = word). MASK clears cells outside the grid: `colmask` holds the
+// lane's in-grid bits, [row_lo, row_hi) the in-grid window rows.
+template <bool MASK>
+MSL_DEV void life_bits_strip(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, int r0, int lane,
+                             uint32_t colmask, int row_lo, int row_hi) {
+    uint32_t fs[kLifeStrip + 2], fc[kLifeStrip + 2], hs[kLifeStrip + 2], hc[kLifeStrip + 2], alive[kLifeStrip + 2];
 #pragma unroll
-        for (int k = 0; k < kLifeStrip + 2; k++) {
-            const uint32_t *row = src + (r0 - 1 + k) * Wd::kNW + w;
-            c[k] = row[0];
-            h[k] = life_hsum(row[-1], c[k], row[1]);
-        }
-        const uint32_t colmask = MASK ? life_colmask(wx0, w, cols) : 0u;
+    for (int k = 0; k < kLifeStrip + 2; k++) {
+        const uint32_t *row = src + (r0 - 1 + k) * kLifePitch + 1 + lane;
+        const uint32_t l = row[-1], c = row[0], r = row[1];
+        const uint32_t lv = __funnelshift_l(l, c, 1);  // bit i: cell to the left of cell i
+        const uint32_t rv = __funnelshift_r(c, r, 1);  // bit i: cell to the right
+        fs[k] = xor3(lv, c, rv);                       // three-cell row sum, ones
+        fc[k] = maj3(lv, c, rv);                       // and twos
+        hs[k] = lv ^ rv;                               // left + right only
+        hc[k] = lv & rv;
+        alive[k] = c;
+    }
 #pragma unroll
-        for (int k = 0; k < kLifeStrip; k++) {
-            const uint32_t sum = h[k] + h[k + 1] + h[k + 2] - c[k + 1];  // the eight neighbours
-            uint32_t v = life_rule4(sum, c[k + 1]);
-            if (MASK) v = (r0 + k >= row_lo && r0 + k < row_hi) ? (v & colmask) : 0u;
-            dst[(r0 + k) * Wd::kNW + w] = v;
-        }
+    for (int k = 1; k <= kLifeStrip; k++) {
+        // count = (fs[k-1] + hs[k] + fs[k+1]) + 2 (fc[k-1] + hc[k] + fc[k+1])
+        const uint32_t c0 = xor3(fs[k - 1], hs[k], fs[k + 1]);
+        const uint32_t k1 = maj3(fs[k - 1], hs[k], fs[k + 1]);
+        const uint32_t t = xor3(fc[k - 1], hc[k], fc[k + 1]);
+        const uint32_t u = maj3(fc[k - 1], hc[k], fc[k + 1]);
+        const uint32_t c1 = t ^ k1, c2 = u ^ (t & k1);
+        uint32_t v = c1 & ~c2 & (c0 | alive[k]);
+        const int rr = r0 + k - 1;
+        if (MASK) v = (rr >= row_lo && rr < row_hi) ? (v & colmask) : 0u;
+        dst[rr * kLifePitch + 1 + lane] = v;
     }
 }
 
-template <int D>
-__global__ void __launch_bounds__(kLifeThreads)
-    life_packed_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, int rows, int cols) {
-    using Wd = LifeWindow<D>;
-    __shared__ uint32_t buf[2][Wd::kWords];
+// Bits of the lane's window word (cells gx0 .. gx0 + 31) that lie in [0, cols).
+MSL_DEV uint32_t life_colmask(int gx0, int cols) {
+    const int lo = max(0, -gx0), hi = min(32, cols - gx0);
+    if (hi <= lo) return 0u;
+    return hi - lo == 32 ? 0xFFFFFFFFu : ((1u << (hi - lo)) - 1u) << lo;
+}
+
+static __global__ void __launch_bounds__(kLifeThreads)
+    life_bits_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, int rows, int cols, int depth) {
+    extern __shared__ uint32_t life_smem[];
+    const int th = kLifeBY + 2 * depth;  // window rows
+    uint32_t *src = life_smem, *dst = life_smem + th * kLifePitch;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int x0 = blockIdx.x * kLifeBX, y0 = blockIdx.y * kLifeBY;
-    const int wx0 = x0 - Wd::kHX, wy0 = y0 - D;
-    // stage: 16-byte loads, four at a time in flight per thread; byte i of
-    // word w = cell 4w + i
-    constexpr int kIter = (Wd::kWords + kLifeThreads - 1) / kLifeThreads;
+    const int wx0 = x0 - 32, wy0 = y0 - depth;  // window origin: one word, `depth` rows of halo
+    const bool cols_in = wx0 >= 0 && wx0 + 32 * kLifeWords <= cols;
+    // zero pads either side of every row of both buffers
+    for (int i = threadIdx.x; i < 2 * th; i += kLifeThreads) {
+        const int at = (i >> 1) * kLifePitch + ((i & 1) ? kLifePitch - 1 : 0);
+        src[at] = 0u;
+        dst[at] = 0u;
+    }
+    // stage: a warp packs whole window rows; word j of a row is the ballot of
+    // cells 32 j .. 32 j + 31, kept by lane j
+    for (int r = warp; r < th; r += kLifeWarps) {
+        const int gy = wy0 + r;
+        uint32_t mine = 0u;
+        if (gy >= 0 && gy < rows) {
+            const int32_t *row = in + (size_t)gy * cols + wx0 + lane;
 #pragma unroll
-    for (int j0 = 0; j0 < kIter; j0 += 4) {
-        int4 v[4];
+            for (int j0 = 0; j0 < kLifeWords; j0 += kLifeLoadBatch) {
+                int v[kLifeLoadBatch];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int i = threadIdx.x + (j0 + u) * kLifeThreads;
-            v[u] = make_int4(0, 0, 0, 0);
-            if (j0 + u < kIter && i < Wd::kWords) {
-                const int r = i / Wd::kNW, w = i - r * Wd::kNW;
-                const int gy = wy0 + r, gx = wx0 + 4 * w;
-                if (gy >= 0 && gy < rows && gx >= 0 && gx < cols)
-                    v[u] = __ldg(reinterpret_cast<const int4 *>(in + (size_t)gy * cols + gx));
+                for (int u = 0; u < kLifeLoadBatch; u++) {
+                    const int gx = wx0 + 32 * (j0 + u) + lane;
+                    v[u] = (cols_in || (gx >= 0 && gx < cols)) ? __ldg(row + 32 * (j0 + u)) : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < kLifeLoadBatch; u++) {
+                    const uint32_t b = __ballot_sync(0xFFFFFFFFu, v[u] != 0);
+                    if (lane == j0 + u) mine = b;
+                }
             }
         }
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int i = threadIdx.x + (j0 + u) * kLifeThreads;
-            if (j0 + u < kIter && i < Wd::kWords)
-                buf[0][i] = __byte_perm(__byte_perm(v[u].x, v[u].y, 0x0040), __byte_perm(v[u].z, v[u].w, 0x0040), 0x5410);
-        }
+        src[r * kLifePitch + 1 + lane] = mine;
     }
-    // the edge words of the second buffer are never computed: keep them 0
-    for (int i = threadIdx.x; i < 2 * Wd::kTH; i += kLifeThreads)
-        buf[1][(i >> 1) * Wd::kNW + ((i & 1) ? Wd::kNW - 1 : 0)] = 0u;
     __syncthreads();
-    const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 + Wd::kP <= cols && wy0 + Wd::kTH <= rows;
+    const bool interior = cols_in && wy0 >= 0 && wy0 + th <= rows;
     const int row_lo = -wy0, row_hi = rows - wy0;  // window rows inside the grid
-#pragma unroll
-    for (int s = 1; s <= D; s++) {
-        const uint32_t *src = buf[(s - 1) & 1];
-        uint32_t *dst = buf[s & 1];
-        if (interior) life_generation<D, false>(src, dst, s, wx0, cols, row_lo, row_hi);
-        else life_generation<D, true>(src, dst, s, wx0, cols, row_lo, row_hi);
-        __syncthreads();
-    }
-    // write the block as int32: a warp stores one 128-cell row
-    const uint32_t *res = buf[D & 1];
-    constexpr int kBW = kLifeBX / 4, wb = Wd::kHX / 4;  // words per block row, first word of the block
-#pragma unroll
-    for (int j = 0; j < kLifeBX * kLifeBY / 4 / kLifeThreads; j++) {
-        const int t = threadIdx.x + j * kLifeThreads;
-        const int ry = t / kBW, wx = t - ry * kBW;
-        const int gy = y0 + ry, gx = x0 + 4 * wx;
-        if (gy < rows && gx < cols) {
-            const uint32_t v = res[(D + ry) * Wd::kNW + wb + wx];
-            *reinterpret_cast<int4 *>(out + (size_t)gy * cols + gx) =
-                make_int4(__byte_perm(v, 0, 0x4440), __byte_perm(v, 0, 0x4441), __byte_perm(v, 0, 0x4442),
-                          __byte_perm(v, 0, 0x4443));
+    const uint32_t colmask = interior ? 0xFFFFFFFFu : life_colmask(wx0 + 32 * lane, cols);
+    for (int s = 1; s <= depth; s++) {
+        // generation s: rows [s, th - s); the last strip ends at the last row
+        const int nrows = th - 2 * s, ns = (nrows + kLifeStrip - 1) / kLifeStrip;
+        for (int sidx = warp; sidx < ns; sidx += kLifeWarps) {
+            const int r0 = s + min(sidx * kLifeStrip, nrows - kLifeStrip);
+            if (interior) life_bits_strip<false>(src, dst, r0, lane, 0u, 0, 0);
+            else life_bits_strip<true>(src, dst, r0, lane, colmask, row_lo, row_hi);
         }
+        __syncthreads();
+        uint32_t *t = src;
+        src = dst;
+        dst = t;
+    }
+    // write the block as int32: lane = cell within a word, 128-byte stores
+    for (int ry = warp; ry < kLifeBY && y0 + ry < rows; ry += kLifeWarps) {
+        const uint32_t *words = src + (depth + ry) * kLifePitch + 2;  // window word 1 = block word 0
+        int32_t *o = out + (size_t)(y0 + ry) * cols + x0 + lane;
+#pragma unroll 6
+        for (int j = 0; j < kLifeBW; j++)
+            if (x0 + 32 * j + lane < cols) o[32 * j] = (int32_t)((words[j] >> lane) & 1u);
     }
 }
 
-template <int D>
-inline cudaError_t launch_life_packed_d(const int32_t *in, int32_t *out, int rows, int cols, cudaStream_t st) {
-    dim3 grid((cols + kLifeBX - 1) / kLifeBX, (rows + kLifeBY - 1) / kLifeBY);
-    life_packed_kernel<D><<<grid, kLifeThreads, 0, st>>>(in, out, rows, cols);
-    return cudaGetLastError();
-}
-
-// `depth` Life generations from `in` (every cell 0 or 1) to `out`, neutral 0.
-// Needs whole 16-byte words per row (cols a multiple of 4, both buffers
-// 16-byte aligned), distinct buffers and 1 <= depth <= kLifeMaxDepth; returns
+// `depth` Life generations from `in` (every cell 0 or 1) to `out`, neutral 0,
+// for 1 <= depth <= kLifeMaxDepth and distinct buffers; returns
 // cudaErrorNotSupported otherwise (the caller then runs the cell-by-cell
 // kernels).
 inline cudaError_t launch_life_packed(const int32_t *in, int32_t *out, int rows, int cols, int depth,
                                       cudaStream_t st) {
-    if (depth < 1 || depth > kLifeMaxDepth || (cols & 3) || ((uintptr_t)in & 15) || ((uintptr_t)out & 15) ||
-        in == out || (rows + kLifeBY - 1) / kLifeBY > 65535)
-        return cudaErrorNotSupported;
-    switch (depth) {
-        case 1: return launch_life_packed_d<1>(in, out, rows, cols, st);
-        case 2: return launch_life_packed_d<2>(in, out, rows, cols, st);
-        case 3: return launch_life_packed_d<3>(in, out, rows, cols, st);
-        case 4: return launch_life_packed_d<4>(in, out, rows, cols, st);
-        case 5: return launch_life_packed_d<5>(in, out, rows, cols, st);
-        case 6: return launch_life_packed_d<6>(in, out, rows, cols, st);
-        case 7: return launch_life_packed_d<7>(in, out, rows, cols, st);
-        case 8: return launch_life_packed_d<8>(in, out, rows, cols, st);
-        case 9: return launch_life_packed_d<9>(in, out, rows, cols, st);
-        case 10: return launch_life_packed_d<10>(in, out, rows, cols, st);
-        case 11: return launch_life_packed_d<11>(in, out, rows, cols, st);
-        case 12: return launch_life_packed_d<12>(in, out, rows, cols, st);
-        case 13: return launch_life_packed_d<13>(in, out, rows, cols, st);
-        case 14: return launch_life_packed_d<14>(in, out, rows, cols, st);
-        case 15: return launch_life_packed_d<15>(in, out, rows, cols, st);
-        default: return launch_life_packed_d<16>(in, out, rows, cols, st);
-    }
+    const int gy = (rows + kLifeBY - 1) / kLifeBY;
+    if (depth < 1 || depth > kLifeMaxDepth || in == out || gy > 65535) return cudaErrorNotSupported;
+    const size_t smem = life_bits_smem(depth);  // <= 34816 bytes
+    dim3 grid((cols + kLifeBX - 1) / kLifeBX, gy);
+    life_bits_kernel<<<grid, kLifeThreads, smem, st>>>(in, out, rows, cols, depth);
+    return cudaGetLastError();
 }
 
 }  // namespace gpu

@@ -50,12 +50,13 @@ def test_heat2d_fused_with_neutral(gpu, depth, d):
     assert res == want_res
 
 
-@pytest.mark.parametrize("d", [1, 2, 3, 4, 5, 6, 7, 8, 9, 12, 16])
-@pytest.mark.parametrize("shape", [(64, 80), (1000, 1024), (300, 1028), (130, 998), (7, 4)], ids=str)
+@pytest.mark.parametrize("d", [1, 2, 3, 4, 5, 6, 7, 8, 9, 12, 16, 24, 31, 32])
+@pytest.mark.parametrize("shape", [(64, 80), (1000, 1024), (300, 1028), (130, 998), (7, 4), (200, 1925), (129, 961)],
+                         ids=str)
 def test_life_fused(gpu, depth, d, shape):
-    """Every launch after the first runs the packed kernel where the width
-    allows it (cols a multiple of 4), the cell-by-cell kernels otherwise; the
-    iteration count leaves a remainder launch of 3 generations."""
+    """The first launch runs one generation cell by cell, every later one d
+    generations on bit-packed cells; the iteration count leaves a remainder
+    launch of 2 generations. Widths around the 960-cell block."""
     depth(d)
     board = W.life_board(*shape, seed=d)
     a, b = gpu.DeviceArray.from_host(board), gpu.DeviceArray(board.shape, np.int32)
@@ -71,6 +72,24 @@ def test_bf16_fused(gpu, depth):
     want, _, want_res = O.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, h, 1, 0.0, 9)
     assert bits_equal(last.download(), want)
     assert res == want_res
+
+
+@pytest.mark.parametrize("d", [8, 32])
+def test_life_fused_with_residual(gpu, depth, d):
+    """A residual makes the last launch run its generations cell by cell."""
+    depth(d)
+    board = W.life_board(100, 200, seed=d)
+    a, b = gpu.DeviceArray.from_host(board), gpu.DeviceArray(board.shape, np.int32)
+    last, res = gpu.stencil2d_iterate(gpu.MSL_ST2_LIFE, a, b, 1, 0, 2 * d + 5)
+    want, _, want_res = O.stencil2d_iterate(gpu.MSL_ST2_LIFE, board, 1, 0, 2 * d + 5)
+    assert bits_equal(last.download(), want)
+    assert res == want_res
+
+
+def test_depth_limit(gpu, depth):
+    with pytest.raises(gpu.MslError) as e:
+        depth(33)
+    assert e.value.code == gpu.MSL_ERR_INVALID_ARGUMENT
 
 
 def test_too_deep_is_an_error(gpu, depth):
