@@ -12,6 +12,7 @@ import math
 import numpy as np
 import pytest
 
+from muesli4_gb300 import abi as A
 from muesli4_gb300 import workloads as W
 from oracle import pyoracle as O
 
@@ -78,11 +79,23 @@ def test_box_mean_8192(gpu, r):
     assert np.array_equal(got[ys, xs], want)
 
 
-def test_life_8192_200_steps(gpu):
+@pytest.fixture(scope="module")
+def life_8192():
     board = W.life_board(8192, 8192, 42)
-    a, b = gpu.DeviceArray.from_host(board), gpu.DeviceArray(board.shape, np.int32)
-    last, _ = gpu.stencil2d_iterate(gpu.MSL_ST2_LIFE, a, b, 1, 0, 200, residual=False)
-    want = O.stencil2d_iterate(gpu.MSL_ST2_LIFE, board, 1, 0, 200)[0]
+    return board, O.stencil2d_iterate(A.MSL_ST2_LIFE, board, 1, 0, 200)[0]
+
+
+@pytest.mark.parametrize("depth", [0, 8, 32])
+def test_life_8192_200_steps(gpu, life_8192, depth):
+    """Generations per launch: 0 = the autotuner's record or 1; 8 and 32 run
+    the bit-packed kernel after the first generation."""
+    board, want = life_8192
+    gpu.set_temporal_depth(depth)
+    try:
+        a, b = gpu.DeviceArray.from_host(board), gpu.DeviceArray(board.shape, np.int32)
+        last, _ = gpu.stencil2d_iterate(gpu.MSL_ST2_LIFE, a, b, 1, 0, 200, residual=False)
+    finally:
+        gpu.set_temporal_depth(0)
     assert np.array_equal(last.download(), want)
 
 
