@@ -842,7 +842,7 @@ def life_launches(steps, depth):
 
 DRAM_TRAFFIC_PER_LAUNCH = {
     "heat3d": 1027.49e6,         # profiles/heat7_stencil3d_512.md (one sweep of 512^3)
-    "life": 495.25e6,            # profiles/life8_stencil2d_8192.md (two sweeps of 8192^2)
+    "life": 480.17e6,            # profiles/life_bits_stencil2d_8192.md (32 generations of 8192^2)
     "box_mean_r1-10": 500.23e6,  # profiles/boxmean_r10_stencil2d_8192.md (r = 10)
 }
 
@@ -962,8 +962,8 @@ def main():
     # DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum +
     # dram__bytes_write.sum) from the ncu captures summarised in profiles/.
     traffic = DRAM_TRAFFIC_PER_LAUNCH.get(p.name)
-    if p.name == "life" and getattr(w, "tuned", {}).get("life_temporal_depth") != 8:
-        traffic = None  # captured at temporal depth 8
+    if p.name == "life" and getattr(w, "tuned", {}).get("life_temporal_depth") != 32:
+        traffic = None  # captured at temporal depth 32
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:

@@ -89,6 +89,26 @@ MSL_DEV void life_bits_strip(const uint32_t *__restrict__ src, uint32_t *__restr
     }
 }
 
+// One window row: `row` points at the lane's cell of word 0, `gx` is its
+// column; CHECK loads only cells inside [0, cols).
+template <bool CHECK>
+MSL_DEV void life_stage_row(const int32_t *__restrict__ row, uint32_t *words, int lane, int gx, int cols) {
+#pragma unroll
+    for (int j0 = 0; j0 < kLifeWords; j0 += kLifeLoadBatch) {
+        int v[kLifeLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLifeLoadBatch; u++) {
+            const int x = gx + 32 * (j0 + u);
+            v[u] = (!CHECK || (x >= 0 && x < cols)) ? __ldg(row + 32 * (j0 + u)) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < kLifeLoadBatch; u++) {
+            const uint32_t b = __ballot_sync(0xFFFFFFFFu, v[u] != 0);
+            if (lane == 0) words[j0 + u] = b;
+        }
+    }
+}
+
 // Bits of the lane's window word (cells gx0 .. gx0 + 31) that lie in [0, cols).
 MSL_DEV uint32_t life_colmask(int gx0, int cols) {
     const int lo = max(0, -gx0), hi = min(32, cols - gx0);
@@ -96,7 +116,7 @@ MSL_DEV uint32_t life_colmask(int gx0, int cols) {
     return hi - lo == 32 ? 0xFFFFFFFFu : ((1u << (hi - lo)) - 1u) << lo;
 }
 
-static __global__ void __launch_bounds__(kLifeThreads)
+static __global__ void __launch_bounds__(kLifeThreads, 8)
     life_bits_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, int rows, int cols, int depth) {
     extern __shared__ uint32_t life_smem[];
     const int th = kLifeBY + 2 * depth;  // window rows
@@ -112,28 +132,22 @@ static __global__ void __launch_bounds__(kLifeThreads)
         dst[at] = 0u;
     }
     // stage: a warp packs whole window rows; word j of a row is the ballot of
-    // cells 32 j .. 32 j + 31, kept by lane j
-    for (int r = warp; r < th; r += kLifeWarps) {
+    // cells 32 j .. 32 j + 31, stored by lane 0 (rows and words outside the
+    // grid are 0). Rows [kLifeBY, th) of this window are rows [0, 2 depth) of
+    // the window below: taking them in the order 0, kLifeBY, 1, kLifeBY + 1,
+    // ... makes both CTAs read each shared row at about the same time, so the
+    // second read finds it in L2.
+    for (int i = warp; i < th; i += kLifeWarps) {
+        const int r = i < 4 * depth ? (i >> 1) + ((i & 1) ? kLifeBY : 0) : i - 2 * depth;
         const int gy = wy0 + r;
-        uint32_t mine = 0u;
-        if (gy >= 0 && gy < rows) {
-            const int32_t *row = in + (size_t)gy * cols + wx0 + lane;
-#pragma unroll
-            for (int j0 = 0; j0 < kLifeWords; j0 += kLifeLoadBatch) {
-                int v[kLifeLoadBatch];
-#pragma unroll
-                for (int u = 0; u < kLifeLoadBatch; u++) {
-                    const int gx = wx0 + 32 * (j0 + u) + lane;
-                    v[u] = (cols_in || (gx >= 0 && gx < cols)) ? __ldg(row + 32 * (j0 + u)) : 0;
-                }
-#pragma unroll
-                for (int u = 0; u < kLifeLoadBatch; u++) {
-                    const uint32_t b = __ballot_sync(0xFFFFFFFFu, v[u] != 0);
-                    if (lane == j0 + u) mine = b;
-                }
-            }
+        uint32_t *words = src + r * kLifePitch + 1;
+        if (gy < 0 || gy >= rows) {
+            words[lane] = 0u;
+            continue;
         }
-        src[r * kLifePitch + 1 + lane] = mine;
+        const int32_t *row = in + (size_t)gy * cols + wx0 + lane;
+        if (cols_in) life_stage_row<false>(row, words, lane, 0, 0);
+        else life_stage_row<true>(row, words, lane, wx0 + lane, cols);
     }
     __syncthreads();
     const bool interior = cols_in && wy0 >= 0 && wy0 + th <= rows;
@@ -153,12 +167,13 @@ static __global__ void __launch_bounds__(kLifeThreads)
         dst = t;
     }
     // write the block as int32: lane = cell within a word, 128-byte stores
+    const bool block_in = x0 + kLifeBX <= cols;
     for (int ry = warp; ry < kLifeBY && y0 + ry < rows; ry += kLifeWarps) {
         const uint32_t *words = src + (depth + ry) * kLifePitch + 2;  // window word 1 = block word 0
         int32_t *o = out + (size_t)(y0 + ry) * cols + x0 + lane;
-#pragma unroll 6
-        for (int j = 0; j < kLifeBW; j++)
-            if (x0 + 32 * j + lane < cols) o[32 * j] = (int32_t)((words[j] >> lane) & 1u);
+        const int jn = block_in ? kLifeBW : min(kLifeBW, (cols - x0 - lane + 31) / 32);  // words with this lane's cell inside
+#pragma unroll 5
+        for (int j = 0; j < jn; j++) o[32 * j] = (int32_t)((words[j] >> lane) & 1u);
     }
 }
 
