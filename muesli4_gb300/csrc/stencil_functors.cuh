@@ -128,7 +128,10 @@ struct StLife {
 // heat3D: ((((((0 + W) + E) + N) + S) + B) + F) / 6 (examples/heatdiffusion.cpp:55-65).
 template <typename T> struct StHeat7 {
     static constexpr bool kStar7 = true;
-    __device__ __forceinline__ T star7(T w, T e, T n, T s, T b, T f) const {
+    // star7 == sum7 / 6 correctly rounded (kernels that split the two take
+    // the division's fast path for whole warps at once)
+    static constexpr bool kSum7Div6 = std::is_same<T, float>::value;
+    __device__ __forceinline__ T sum7(T w, T e, T n, T s, T b, T f) const {
         T v = T(0);
         v = Arith<T>::add(v, w);
         v = Arith<T>::add(v, e);
@@ -136,6 +139,10 @@ template <typename T> struct StHeat7 {
         v = Arith<T>::add(v, s);
         v = Arith<T>::add(v, b);
         v = Arith<T>::add(v, f);
+        return v;
+    }
+    __device__ __forceinline__ T star7(T w, T e, T n, T s, T b, T f) const {
+        const T v = sum7(w, e, n, s, b, f);
         if constexpr (std::is_same<T, float>::value) return div6_rn(v);  // == v / 6, correctly rounded
         else return div_rn<T>(v, T(6));
     }

@@ -230,14 +230,22 @@ namespace gpu {
 // checked against IEEE division for every one of the 2^32 float inputs by the
 // GPU test suite. The method needs a normal quotient, so inputs below 2^-122
 // in magnitude take IEEE division; infinities and NaNs pass through q.
-MSL_DEV float div6_rn(float x) {
+// Inputs for which the method below is exact: 2^-122 <= |x| <= FLT_MAX.
+MSL_DEV bool div6_in_range(float x) {
     const float ax = fabsf(x);
-    // tiny (< 2^-122), infinite and NaN inputs: IEEE division
-    if (!(ax >= 1.88079096131566e-37f && ax <= 3.40282346638528859812e38f)) return __fdiv_rn(x, 6.0f);
+    return ax >= 1.88079096131566e-37f && ax <= 3.40282346638528859812e38f;
+}
+// The method alone (exact for div6_in_range inputs).
+MSL_DEV float div6_core(float x) {
     const float zh = 0.16666667163372039794921875f;  // RN(1/6)
     const float q = __fmul_rn(x, zh);
     const float r = __fmaf_rn(-q, 6.0f, x);
     return __fmaf_rn(r, zh, q);
+}
+MSL_DEV float div6_rn(float x) {
+    // tiny (< 2^-122), infinite and NaN inputs: IEEE division
+    if (!div6_in_range(x)) return __fdiv_rn(x, 6.0f);
+    return div6_core(x);
 }
 
 }  // namespace gpu

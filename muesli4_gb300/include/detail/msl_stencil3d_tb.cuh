@@ -39,6 +39,36 @@ inline size_t stencil3d_ztb_smem() {
     return (size_t)kStHeader + (size_t)(kZtbIn + kZtbMid) * kZtbPlane * sizeof(float);
 }
 
+template <class Fn, class = void> struct IsSum7Div6 : std::false_type {};
+template <class Fn> struct IsSum7Div6<Fn, std::void_t<decltype(Fn::kSum7Div6)>> : std::bool_constant<Fn::kSum7Div6> {};
+
+// One cell of a sweep. A functor whose value is sum7 / 6 (heat3D) takes the
+// division's fast path here; `ok` is cleared when a live cell's sum lies
+// outside that path's range, and ztb_fixup redoes those cells.
+template <class Fn>
+MSL_DEV float ztb_cell(const Fn &fn, float w, float e, float n, float s, float b, float f, bool live, float &sum,
+                       bool &ok) {
+    if constexpr (IsSum7Div6<Fn>::value) {
+        sum = fn.sum7(w, e, n, s, b, f);
+        ok = ok && (!live || div6_in_range(sum));
+        return div6_core(sum);
+    } else {
+        return fn.star7(w, e, n, s, b, f);
+    }
+}
+
+// One vote per warp and sweep: if any lane holds a sum outside the fast
+// division's range, those cells take IEEE division.
+template <class Fn, int N>
+MSL_DEV void ztb_fixup(const Fn &, bool ok, const bool (&live)[N], const float (&sum)[N], float (&v)[N]) {
+    if constexpr (IsSum7Div6<Fn>::value) {
+        if (__all_sync(0xFFFFFFFFu, ok)) return;
+#pragma unroll
+        for (int j = 0; j < N; j++)
+            if (live[j] && !div6_in_range(sum[j])) v[j] = __fdiv_rn(sum[j], 6.0f);
+    }
+}
+
 template <class Fn>
 __global__ void __launch_bounds__(kT3Threads, 4)
     stencil3d_ztb_kernel(const __grid_constant__ CUtensorMap tmap, float *out, int depth, int rows, int cols, Fn fn,
@@ -55,6 +85,7 @@ __global__ void __launch_bounds__(kT3Threads, 4)
     const int cx = 4 + (warp & 1) * 32 + lane, cy = 2 + (warp >> 1) * kT3RPT;
     const int gx = wx0 + cx, gy0 = wy0 + cy;
     const bool x_in = gx < cols;
+    const bool xy_in = x0 + kT3BX <= cols && y0 + kT3BY <= rows;  // every thread's own cells lie in the grid
     // margin cell of the first sweep (threads 0 .. 163): window columns 3 and
     // 68 for rows 1..18, and rows 1 and 18 for columns 4..67
     int mx = -1, my = -1;
@@ -116,28 +147,38 @@ __global__ void __launch_bounds__(kT3Threads, 4)
     // First sweep at plane p for this thread's cells and margin cell from
     // input planes pb = p-1, pc = p, pf = p+1 (staged; the own column's values
     // in registers cb, cc, cf). Writes the intermediate plane (0 outside the
-    // grid) to `m` and this thread's values to `res`.
-    auto first_sweep = [&](int p, const float *pb, const float *pc, const float *pf, const Col &cb, const Col &cc,
-                           const Col &cf, float *m, Col &res) {
-        const bool p_in = p >= 0 && p < depth;
+    // grid) to `m` and this thread's values to `res`. FULL: plane p and the
+    // thread's own cells lie inside the grid (no per-cell tests).
+    auto first_sweep = [&](auto full_tag, int p, const float *pb, const float *pc, const float *pf, const Col &cb,
+                           const Col &cc, const Col &cf, float *m, Col &res) {
+        constexpr bool FULL = decltype(full_tag)::value;
+        const bool p_in = FULL || (p >= 0 && p < depth);
         const float *q = pc + cy * kZtbPitch + cx;
         const float n = q[-kZtbPitch], s = q[kT3RPT * kZtbPitch];
+        float sum[kT3RPT + 1], v[kT3RPT + 1];
+        bool live[kT3RPT + 1];
+        bool ok = true;
 #pragma unroll
         for (int j = 0; j < kT3RPT; j++) {
-            float v = 0.0f;
-            if (p_in && x_in && gy0 + j < rows) {
-                const float w = q[j * kZtbPitch - 1], e = q[j * kZtbPitch + 1];
-                v = fn.star7(w, e, j == 0 ? n : cc[j - 1], j == kT3RPT - 1 ? s : cc[j + 1], cb[j], cf[j]);
-            }
-            res[j] = v;
-            m[(cy + j) * kZtbPitch + cx] = v;
+            live[j] = FULL || (p_in && x_in && gy0 + j < rows);
+            v[j] = ztb_cell(fn, q[j * kZtbPitch - 1], q[j * kZtbPitch + 1], j == 0 ? n : cc[j - 1],
+                            j == kT3RPT - 1 ? s : cc[j + 1], cb[j], cf[j], live[j], sum[j], ok);
         }
-        if (has_margin) {
-            const int o = my * kZtbPitch + mx;
-            float v = 0.0f;
-            if (p_in && m_in) v = fn.star7(pc[o - 1], pc[o + 1], pc[o - kZtbPitch], pc[o + kZtbPitch], pb[o], pf[o]);
-            m[o] = v;
+        const int o = has_margin ? my * kZtbPitch + mx : 0;
+        live[kT3RPT] = has_margin && p_in && m_in;
+        v[kT3RPT] = 0.0f;
+        sum[kT3RPT] = 0.0f;
+        if (has_margin)
+            v[kT3RPT] = ztb_cell(fn, pc[o - 1], pc[o + 1], pc[o - kZtbPitch], pc[o + kZtbPitch], pb[o], pf[o],
+                                 live[kT3RPT], sum[kT3RPT], ok);
+        ztb_fixup(fn, ok, live, sum, v);
+#pragma unroll
+        for (int j = 0; j < kT3RPT; j++) {
+            const float x = live[j] ? v[j] : 0.0f;
+            res[j] = x;
+            m[(cy + j) * kZtbPitch + cx] = x;
         }
+        if (has_margin) m[o] = live[kT3RPT] ? v[kT3RPT] : 0.0f;
     };
 
     // Registers: three input columns and three intermediate columns whose
@@ -156,13 +197,13 @@ __global__ void __launch_bounds__(kT3Threads, 4)
             load_col(ca, in_at(k0));
             load_col(cb, in_at(k1));
             load_col(cc, in_at(k2));
-            first_sweep(zb - 1, in_at(k0), in_at(k1), in_at(k2), ca, cb, cc, mid_at(0), mb);
+            first_sweep(std::false_type{}, zb - 1, in_at(k0), in_at(k1), in_at(k2), ca, cb, cc, mid_at(0), mb);
             ok = wait_slot(k3);
         }
         ok = __syncthreads_and(ok);
         if (ok) {
             load_col(ca, in_at(k3));  // plane zb+1 takes the place of zb-2
-            first_sweep(zb, in_at(k1), in_at(k2), in_at(k3), cb, cc, ca, mid_at(1), mc);
+            first_sweep(std::false_type{}, zb, in_at(k1), in_at(k2), in_at(k3), cb, cc, ca, mid_at(1), mc);
             ok = wait_slot(4);  // input plane zb+2, read by step zb
         }
         ok = __syncthreads_and(ok);  // intermediate planes zb-1 and zb visible
@@ -183,21 +224,32 @@ __global__ void __launch_bounds__(kT3Threads, 4)
         // the slot of plane t-2 is free since step t-2: load plane t+4 into it
         if (threadIdx.x == 0 && t + kZtbIn - 2 <= ze + 1) issue(t + kZtbIn - 2);
         load_col(xf, in_at(s2));
-        first_sweep(t + 1, in_at(s0), in_at(s1), in_at(s2), xb, xc, xf, mid_at(m2), yf);
+        if (xy_in && t + 1 < depth)
+            first_sweep(std::true_type{}, t + 1, in_at(s0), in_at(s1), in_at(s2), xb, xc, xf, mid_at(m2), yf);
+        else
+            first_sweep(std::false_type{}, t + 1, in_at(s0), in_at(s1), in_at(s2), xb, xc, xf, mid_at(m2), yf);
         // second sweep at plane t from intermediate planes t-1, t, t+1
         const float *q = mid_at(m1) + cy * kZtbPitch + cx;
         const float n = q[-kZtbPitch], s = q[kT3RPT * kZtbPitch];
+        float sum[kT3RPT], v[kT3RPT];
+        bool live[kT3RPT];
+        bool ok2 = true;
+#pragma unroll
+        for (int j = 0; j < kT3RPT; j++) {
+            live[j] = xy_in || (x_in && gy0 + j < rows);
+            v[j] = ztb_cell(fn, q[j * kZtbPitch - 1], q[j * kZtbPitch + 1], j == 0 ? n : yc[j - 1],
+                            j == kT3RPT - 1 ? s : yc[j + 1], yb[j], yf[j], live[j], sum[j], ok2);
+        }
+        ztb_fixup(fn, ok2, live, sum, v);
         float *o = out + ((size_t)t * rows + gy0) * cols + gx;
 #pragma unroll
         for (int j = 0; j < kT3RPT; j++) {
-            const float w = q[j * kZtbPitch - 1], e = q[j * kZtbPitch + 1];
-            const float v = fn.star7(w, e, j == 0 ? n : yc[j - 1], j == kT3RPT - 1 ? s : yc[j + 1], yb[j], yf[j]);
-            if (x_in && gy0 + j < rows) {
+            if (live[j]) {
                 if (want) {
-                    const double d = fabs((double)v - (double)yc[j]);
+                    const double d = fabs((double)v[j] - (double)yc[j]);
                     if (d > dmax || d != d) dmax = d;
                 }
-                o[(size_t)j * cols] = v;
+                o[(size_t)j * cols] = v[j];
             }
         }
         const bool good = __syncthreads_and(t + 1 < ze ? wait_slot(next_in(s2)) : true);  // plane t+3 for step t+1

@@ -358,6 +358,30 @@ def test_stencil3d_heat_z_marching(gpu, shape, sweeps_per_launch):
         gpu.set_stencil3d_depth(1)
 
 
+@pytest.mark.parametrize("sweeps_per_launch", [2, 1])
+def test_stencil3d_heat_special_values(gpu, sweeps_per_launch):
+    """Sums outside the fast division's range (zero, below 2^-122, subnormal,
+    infinite) and negative cells: those cells take IEEE division, the rest of
+    the warp the fast path; bit-identical to the oracle either way."""
+    rng = np.random.default_rng(11)
+    x = W.heat_cube(40, 64, 70, seed=5)
+    u = rng.random(x.shape)
+    x[u < 0.01] = np.float32(1e-38)
+    x[(u >= 0.01) & (u < 0.02)] = np.float32(3e-40)
+    x[(u >= 0.02) & (u < 0.025)] = np.float32(np.inf)
+    x[(u >= 0.025) & (u < 0.05)] *= np.float32(-0.3)
+    x[8:16, 16:24, 24:32] = 0.0
+    gpu.set_stencil3d_depth(sweeps_per_launch)
+    try:
+        for iters in (1, 2, 4):
+            a, b = dev(gpu, x), gpu.DeviceArray(x.shape, x.dtype)
+            last, _ = gpu.stencil3d_iterate(gpu.MSL_ST3_HEAT7, a, b, 1, 0.0, iters, residual=False)
+            want = O.stencil3d_iterate(gpu.MSL_ST3_HEAT7, x, 1, 0.0, iters)[0]
+            assert bits_equal(last.download(), want), iters
+    finally:
+        gpu.set_stencil3d_depth(1)
+
+
 @pytest.mark.parametrize("persistent", [0, 1])
 @pytest.mark.parametrize("r", [1, 2, 3])
 @pytest.mark.parametrize("shape", [(9, 10, 11), (24, 20, 68)], ids=str)
