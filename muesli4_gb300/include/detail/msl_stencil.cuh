@@ -70,6 +70,12 @@ template <typename T, typename S = T> class NPLMatrix {
         if (check_ && ((unsigned)x >= (unsigned)width || (unsigned)y >= (unsigned)height)) return neutralValue;
         return gpu::widen<S>(tile_[(y - oy_) * pitch_ + (x - ox_)]);
     }
+    // Unchecked access for strip functors (valid while check_ is false: the
+    // staged window then holds every cell the functor reads): the window
+    // address of cell (x, y); rows are pitch_ apart.
+    __host__ __device__ __forceinline__ const S *window_at(int x, int y) const {
+        return tile_ + (y - oy_) * pitch_ + (x - ox_);
+    }
 };
 
 template <typename T, typename S = T> class PLCube {
@@ -181,6 +187,24 @@ template <typename T> MSL_DEV T heat5_value(T w, T e, T n, T s) {
 // kSt2RPT + 2 values are read once and serve as N, S and centre of the cells.
 template <bool JACOBI, class V, typename T>
 MSL_DEV void heat5_strip(const V &m, int x, int y0, T (&out)[kSt2RPT]) {
+    if (!m.check_) {
+        // the window holds every cell read: address it directly (one pointer,
+        // row offsets by pitch) instead of through the view's checks
+        const auto *p = m.window_at(x, y0 - 1);
+        const int pitch = m.pitch_;
+        T c[kSt2RPT + 2];
+#pragma unroll
+        for (int k = 0; k < kSt2RPT + 2; k++) c[k] = gpu::widen(p[k * pitch]);
+        const bool edge = JACOBI && (x == 0 || x == m.width - 1 || y0 == 0 || y0 + kSt2RPT >= m.height);
+        if (!edge) {
+#pragma unroll
+            for (int j = 0; j < kSt2RPT; j++) {
+                const auto *q = p + (j + 1) * pitch;
+                out[j] = heat5_value<T>(gpu::widen(q[-1]), gpu::widen(q[1]), c[j], c[j + 2]);
+            }
+            return;
+        }
+    }
     T c[kSt2RPT + 2];
 #pragma unroll
     for (int k = 0; k < kSt2RPT + 2; k++) c[k] = m(x, y0 - 1 + k);
