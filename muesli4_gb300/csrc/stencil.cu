@@ -29,7 +29,7 @@ std::atomic<int> g_persistent3d{-1};
 // Sweeps per launch of msl_stencil3d_iterate where the z-marching kernel
 // applies (1 or 2). One sweep per launch is the default: on heat3D 512^3 the
 // one-sweep kernel runs at the HBM roofline (786 GCUPS) while the z-marching
-// kernel, with half the HBM traffic, is bound by instruction issue (651).
+// kernel, with half the HBM traffic, is bound by instruction issue (660).
 std::atomic<int> g_depth3d{1};
 
 template <typename S>
