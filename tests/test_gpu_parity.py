@@ -253,14 +253,39 @@ def test_stencil2d_float(gpu, shape, kind, neutral, tma):
         gpu.set_tma(True)
 
 
+@pytest.mark.parametrize("tma", [True, False], ids=["tma", "plain"])
 @pytest.mark.parametrize("r", [1, 2, 3, 4, 5, 6, 7, 8, 10, 12])
-@pytest.mark.parametrize("shape", [(13, 17), (64, 96), (130, 260)], ids=str)
-def test_stencil2d_box(gpu, r, shape):
+@pytest.mark.parametrize("shape", [(13, 17), (64, 96), (130, 260), (33, 130)], ids=str)
+def test_stencil2d_box(gpu, r, shape, tma):
+    """Radii 1-4, 6, 8, 10 with neutral +0 run the two-columns-per-thread
+    kernel with packed additions; odd widths store column by column."""
     x = W.blur_image(*shape, seed=r)
     d, o = dev(gpu, x), gpu.DeviceArray(x.shape, x.dtype)
-    for kind in (gpu.MSL_ST2_BOXMEAN, gpu.MSL_ST2_BOXSUM):
-        gpu.stencil2d(kind, d, o, r, 0.0)
-        assert bits_equal(o.download(), O.stencil2d(kind, x, r, 0.0)), (kind, r)
+    gpu.set_tma(tma)
+    try:
+        for kind in (gpu.MSL_ST2_BOXMEAN, gpu.MSL_ST2_BOXSUM):
+            gpu.stencil2d(kind, d, o, r, 0.0)
+            assert bits_equal(o.download(), O.stencil2d(kind, x, r, 0.0)), (kind, r)
+    finally:
+        gpu.set_tma(True)
+
+
+@pytest.mark.parametrize("r", [1, 4, 10])
+def test_stencil2d_box_special_values(gpu, r):
+    """Packed additions round each lane like a scalar addition: infinities,
+    subnormals, negative values and a -0 neutral value (which takes the
+    one-column kernel) all match the oracle bit for bit."""
+    rng = np.random.default_rng(r)
+    x = W.blur_image(70, 200, seed=r)
+    u = rng.random(x.shape)
+    x[u < 0.01] = np.float32(np.inf)
+    x[(u >= 0.01) & (u < 0.03)] = np.float32(3e-41)
+    x[(u >= 0.03) & (u < 0.2)] *= np.float32(-1.0)
+    d, o = dev(gpu, x), gpu.DeviceArray(x.shape, x.dtype)
+    for neutral in (0.0, -0.0):
+        for kind in (gpu.MSL_ST2_BOXMEAN, gpu.MSL_ST2_BOXSUM):
+            gpu.stencil2d(kind, d, o, r, neutral)
+            assert bits_equal(o.download(), O.stencil2d(kind, x, r, neutral)), (kind, neutral)
 
 
 def test_stencil2d_box_neutral_and_f64(gpu):
