@@ -677,7 +677,7 @@ def serve_requests(count: int, seed: int = 11):
 
 
 def run_serve(args, dist: Dist):
-    """Served stencil solves (BASELINE configs[4]): Poisson arrivals at rates
+    """Served stencil solves (Jacobi and heat3D requests of mixed sizes): Poisson arrivals at rates
     swept around the plain path's capacity; p50/p99 latency and solves/s of the
     continuously batching server against the one-request-at-a-time GPU path
     (FIFO queue fed the same arrivals; its service times are measured on a
@@ -769,7 +769,7 @@ def run_serve(args, dist: Dist):
 
 
 def run_batch(args, dist: Dist):
-    """Batched solves (BASELINE configs[3]): solves/s of the batched path, the
+    """Batched solves (256 Jacobi grids of mixed sizes): solves/s of the batched path, the
     one-grid-at-a-time GPU path on a size-stratified sample, and the error of
     a sample of results against FP64 sweeps computed by the CPU oracle."""
     from muesli4_gb300 import abi as A
@@ -859,7 +859,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-cap", type=int, default=0, help="sweep cap of the batch workloads")
     ap.add_argument("--batch-grids", type=int, default=0, help="number of grids of the batch workloads")
-    ap.add_argument("--serve-requests", type=int, default=400, help="requests of the serve workload (configs: 10000)")
+    ap.add_argument("--serve-requests", type=int, default=400, help="requests of the serve workload (the full stream: 10000)")
     ap.add_argument("--serve-plain-sample", type=int, default=40)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[0.25, 0.5, 1.0, 2.0])
     ap.add_argument("--temporal-depth", type=int, default=0,
