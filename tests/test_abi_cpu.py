@@ -50,3 +50,16 @@ def test_init_without_a_device_fails_cleanly(lib):
 def test_status_codes_are_distinct():
     codes = [v for k, v in vars(abi).items() if k.startswith("MSL_ERR_")]
     assert len(codes) == len(set(codes)) and all(c < 0 for c in codes)
+
+
+def test_setters_validate_their_arguments(lib):
+    """Process-wide settings need no device; out-of-range values are refused
+    with INVALID_ARGUMENT and leave the setting unchanged."""
+    bad = abi.MSL_ERR_INVALID_ARGUMENT
+    assert lib.msl_set_temporal_depth(33) == bad and lib.msl_set_temporal_depth(-1) == bad
+    assert lib.msl_set_temporal_depth(32) == abi.MSL_OK and lib.msl_set_temporal_depth(0) == abi.MSL_OK
+    assert lib.msl_set_stencil3d_depth(0) == bad and lib.msl_set_stencil3d_depth(3) == bad
+    assert lib.msl_set_stencil3d_depth(2) == abi.MSL_OK and lib.msl_set_stencil3d_depth(1) == abi.MSL_OK
+    assert lib.msl_set_stencil3d_persistent(2) == bad and lib.msl_set_stencil3d_persistent(-2) == bad
+    assert lib.msl_set_stencil3d_persistent(-1) == abi.MSL_OK
+    assert lib.msl_set_tma(0) == abi.MSL_OK and lib.msl_set_tma(1) == abi.MSL_OK
