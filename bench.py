@@ -868,6 +868,8 @@ def main():
                     help="heat3D sweeps per launch: 1 one sweep (default), 2 the z-marching kernel")
     ap.add_argument("--stencil3d-persistent", type=int, default=-1, choices=[-1, 0, 1],
                     help="3-D stencil kernel: 1 persistent, 0 one CTA per block, -1 library default")
+    ap.add_argument("--elements", type=int, default=0,
+                    help="array length of the mapzipfold workload (default 2^28; smaller for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -890,7 +892,8 @@ def main():
     A.init(dist.local_rank)
     A.set_stencil3d_persistent(args.stencil3d_persistent)
     A.set_stencil3d_depth(args.stencil3d_depth)
-    w = WORKLOADS[args.workload](A)
+    w = MapZipFold(A, args.elements) if args.workload == "mapzipfold" and args.elements > 0 \
+        else WORKLOADS[args.workload](A)
     w.fixed_depth = args.temporal_depth  # > 0: no autotuning of the Life depth
     w.setup()
     if args.temporal_depth > 0:  # after setup: overrides the autotuner's record

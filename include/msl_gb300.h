@@ -176,8 +176,13 @@ int msl_fold_absdiff_max(int dtype, const void *a, const void *b, size_t n, doub
  * synchronises. Its scratch is a static device array of 2048 CTA partials
  * (about 41 KiB, held by every device that loads the library until exit), so n
  * is limited to 2^30 elements; larger n fails with MSL_ERR_SIZE_MISMATCH
- * before anything is launched. The first call on each device looks up the
- * array's device address (make that first call before any stream capture).
+ * before anything is launched. Every call looks up the array's device address
+ * in the current context (no allocation). The first call on each device (in
+ * each context) also makes the CUDA runtime load this library's device code
+ * into that context when lazy module loading is on (the default): that
+ * one-time load may allocate device memory and synchronise. Callers that must
+ * never pay either make one warm-up call during set-up, before any stream
+ * capture, or run with CUDA_MODULE_LOADING=EAGER.
  * All calls share the array: calls that overlap on the GPU race and must be
  * serialised by the caller. dtype MSL_F32, MSL_F64 or MSL_I32; op as msl_fold.
  * No counterpart in the reference (its fold allocates per call, src/ds.cpp:772). */

@@ -33,27 +33,30 @@ constexpr size_t kNoAllocMaxElems = (size_t)kNoAllocSlots * kFoldThreads * kMaxP
 
 static __device__ __align__(256) unsigned char g_fold_noalloc_scratch[kNoAllocBytes];
 
-// Per-device set-up, done by the first call on each device (with that device
-// current): the device address of the static array and the SM count.
+// The device address of the static array is looked up on every call, with the
+// caller's device and context current: a module loaded into another context
+// (a plugin host's own context, or the primary context rebuilt after
+// cudaDeviceReset) has its own copy of the array at another address, so an
+// address cached from an earlier call could point at memory this context does
+// not own. The lookup allocates nothing. The SM count is a property of the
+// device and is cached per device ordinal.
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
-void *g_scratch_addr[kMaxDevices];
 int g_sm_count[kMaxDevices];
 
-int setup_device(int dev, void **base, int *sms) {
+int setup_call(int dev, void **base, int *sms) {
     if (dev < 0 || dev >= kMaxDevices) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_fold_noalloc: device %d", dev);
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_fold_noalloc_scratch);
+    if (e != cudaSuccess) return rt::cuda_fail(e, "msl_fold_noalloc: cudaGetSymbolAddress");
     std::lock_guard<std::mutex> g(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_fold_noalloc_scratch);
-        if (e != cudaSuccess) return rt::cuda_fail(e, "msl_fold_noalloc: cudaGetSymbolAddress");
+    if (!g_sm_count[dev]) {
         int n = 0;
         e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return rt::cuda_fail(e, "msl_fold_noalloc: SM count");
         g_sm_count[dev] = n;
-        g_scratch_addr[dev] = p;
     }
-    *base = g_scratch_addr[dev];
+    *base = p;
     *sms = g_sm_count[dev];
     return MSL_OK;
 }
@@ -71,9 +74,10 @@ template <typename T, int OP> cudaError_t launch(const void *in, size_t n, void 
     constexpr int V = vec_width1<T>();
     const bool vec = aligned_to(in, V * sizeof(T));
     const size_t units = vec ? n / V : n;
-    // The usual SM-filling grid, raised when needed so that no thread folds
+    // The usual one-wave grid, raised when needed so that no thread folds
     // more than kMaxPerThread elements; never more CTAs than partial slots.
-    size_t blocks = fold_blocks(units, sms);
+    constexpr int UV = fold_unroll<T, V>(), U1 = fold_unroll<T, 1>();
+    size_t blocks = fold_blocks(units, sms, 2, vec ? UV : U1);
     const size_t need = (n + (size_t)kFoldThreads * kMaxPerThread - 1) / ((size_t)kFoldThreads * kMaxPerThread);
     if (blocks < need) blocks = need;
     if (blocks > (size_t)kNoAllocSlots) blocks = kNoAllocSlots;
@@ -88,12 +92,12 @@ template <typename T, int OP> cudaError_t launch(const void *in, size_t n, void 
     if (e != cudaSuccess) return e;
     if (vec) {
         FoldSrcArray<T, V> src{(const T *)in};
-        fold_kernel<V, kFoldUnroll><<<(unsigned)blocks, kFoldThreads, 0, st>>>(src, n, NoAllocOp<T, OP>{}, partials,
-                                                                               have, ticket, (T *)result, result_have);
+        fold_kernel<V, UV><<<(unsigned)blocks, kFoldThreads, 0, st>>>(src, n, NoAllocOp<T, OP>{}, partials, have,
+                                                                     ticket, (T *)result, result_have);
     } else {
         FoldSrcArray<T, 1> src{(const T *)in};
-        fold_kernel<1, kFoldUnroll><<<(unsigned)blocks, kFoldThreads, 0, st>>>(src, n, NoAllocOp<T, OP>{}, partials,
-                                                                               have, ticket, (T *)result, result_have);
+        fold_kernel<1, U1><<<(unsigned)blocks, kFoldThreads, 0, st>>>(src, n, NoAllocOp<T, OP>{}, partials, have,
+                                                                     ticket, (T *)result, result_have);
     }
     return cudaGetLastError();
 }
@@ -126,7 +130,7 @@ int msl_fold_noalloc(int dtype, int op, const void *in, size_t n, void *result_d
     MSL_TRY_CUDA(cudaGetDevice(&dev), "msl_fold_noalloc: cudaGetDevice");
     void *base = nullptr;
     int sms = 0;
-    if (int e = setup_device(dev, &base, &sms)) return e;
+    if (int e = setup_call(dev, &base, &sms)) return e;
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e;
     switch (dtype) {

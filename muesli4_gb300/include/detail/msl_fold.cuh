@@ -22,8 +22,11 @@ namespace msl {
 namespace gpu {
 
 constexpr int kFoldThreads = 512;
-constexpr int kFoldUnroll = 4;
+constexpr int kFoldUnroll = 4;  // vectors in flight per thread when a value takes more than 16 bytes a vector
 constexpr int kFoldMaxBlocks = 4096;
+// Vectors in flight per thread: 8 when a vector of values fits 16 bytes (128 B
+// in flight per thread), else 4 (the FP64 residual of FP32 / BF16 inputs).
+template <typename R, int V> constexpr int fold_unroll() { return sizeof(R) * V <= 16 ? 8 : kFoldUnroll; }
 
 // Element source over one array.
 template <typename T, int V> struct FoldSrcArray {
@@ -94,7 +97,7 @@ template <typename T, class F> MSL_DEV void block_fold(T &acc, bool &have, const
 }
 
 template <int V, int U, class Src, class F>
-__global__ void __launch_bounds__(kFoldThreads)
+__global__ void __launch_bounds__(kFoldThreads, 2)
     fold_kernel(Src src, size_t n, F f, typename Src::value_type *partials, int *part_have,
                 unsigned *ticket, typename Src::value_type *result, int *result_have) {
     using T = typename Src::value_type;
@@ -162,10 +165,20 @@ __global__ void __launch_bounds__(kFoldThreads)
     }
 }
 
-inline unsigned fold_blocks(size_t units, int sm_count) {
-    size_t per_block = (size_t)kFoldThreads * kFoldUnroll;
+// CTAs of `kernel` (kFoldThreads threads) resident per SM, at least 1.
+template <class K> int fold_occupancy(K kernel) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kFoldThreads, 0) != cudaSuccess || b < 1) b = 1;
+    return b;
+}
+
+// One wave: as many CTAs as fit on the GPU at once (`per_sm` resident per SM),
+// fewer when the input is small. A grid beyond one wave would leave a partial
+// last wave (the grid-stride loop gives every CTA the same work).
+inline unsigned fold_blocks(size_t units, int sm_count, int per_sm = 2, int unroll = kFoldUnroll) {
+    size_t per_block = (size_t)kFoldThreads * unroll;
     size_t b = (units + per_block - 1) / per_block;
-    size_t cap = (size_t)(sm_count > 0 ? sm_count : 152) * 4;  // 4 x 512 threads = a full SM
+    size_t cap = (size_t)(sm_count > 0 ? sm_count : 152) * (size_t)(per_sm > 0 ? per_sm : 1);
     if (cap > (size_t)kFoldMaxBlocks) cap = kFoldMaxBlocks;
     if (b > cap) b = cap;
     return (unsigned)(b ? b : 1);
@@ -199,13 +212,19 @@ cudaError_t launch_fold(size_t n, F f, const FoldScratch &s, cudaStream_t st, in
     using R = typename SrcT<T, V>::value_type;
     static_assert(sizeof(R) <= 16, "fold value type too large for the scratch slots");
     if (V > 1 && vec_ok) {
+        constexpr int U = fold_unroll<R, V>();
+        auto k = fold_kernel<V, U, SrcT<T, V>, F>;
+        static const int occ = fold_occupancy(k);
         SrcT<T, V> src{ptrs...};
-        fold_kernel<V, kFoldUnroll><<<fold_blocks(n / V, sms), kFoldThreads, 0, st>>>(
-            src, n, f, (R *)s.partials, s.part_have, s.ticket, (R *)s.result, s.result_have);
+        k<<<fold_blocks(n / V, sms, occ, U), kFoldThreads, 0, st>>>(src, n, f, (R *)s.partials, s.part_have,
+                                                                    s.ticket, (R *)s.result, s.result_have);
     } else {
+        constexpr int U = fold_unroll<R, 1>();
+        auto k = fold_kernel<1, U, SrcT<T, 1>, F>;
+        static const int occ = fold_occupancy(k);
         SrcT<T, 1> src{ptrs...};
-        fold_kernel<1, kFoldUnroll><<<fold_blocks(n, sms), kFoldThreads, 0, st>>>(
-            src, n, f, (R *)s.partials, s.part_have, s.ticket, (R *)s.result, s.result_have);
+        k<<<fold_blocks(n, sms, occ, U), kFoldThreads, 0, st>>>(src, n, f, (R *)s.partials, s.part_have, s.ticket,
+                                                                (R *)s.result, s.result_have);
     }
     return cudaGetLastError();
 }

@@ -23,6 +23,57 @@ template <typename T, class F> struct PlmCall {
         else return f(y, x, &pl, m.width, m.height);
     }
 };
+// mapStencilMM with a neutral-value functor: the view reads cells outside the
+// matrix from the halo ring the functor filled.
+template <typename T, class F> struct PlmNvfCall {
+    F f;
+    const T *halo;
+    int r;
+    __device__ __forceinline__ T operator()(const NPLMatrix<T> &m, int x, int y) const {
+        PLMatrix<T> pl(m, halo, r);
+        if constexpr (std::is_class<F>::value) return f.F::operator()(y, x, &pl, m.width, m.height);
+        else return f(y, x, &pl, m.width, m.height);
+    }
+};
+// halo[k] = nvf(row, col) for every cell (row, col) of the ring.
+template <typename T, class NVF> __global__ void halo_ring_kernel(T *halo, HaloRing ring, NVF nvf) {
+    const long long n = ring.size(), stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        int row, col;
+        ring.cell(k, row, col);
+        halo[k] = invoke(nvf, row, col);
+    }
+}
+// Device buffer of a container's halo ring, kept between calls. A copy of the
+// container starts without one; a move takes it along.
+struct HaloBuffer {
+    void *p = nullptr;
+    size_t bytes = 0;
+    HaloBuffer() = default;
+    HaloBuffer(const HaloBuffer &) {}
+    HaloBuffer &operator=(const HaloBuffer &) { return *this; }
+    HaloBuffer(HaloBuffer &&o) noexcept : p(o.p), bytes(o.bytes) {
+        o.p = nullptr;
+        o.bytes = 0;
+    }
+    HaloBuffer &operator=(HaloBuffer &&o) noexcept {
+        std::swap(p, o.p);
+        std::swap(bytes, o.bytes);
+        return *this;
+    }
+    ~HaloBuffer() {
+        if (p) msl_free(p);
+    }
+    void *reserve(size_t need) {
+        if (need <= bytes) return p;
+        if (p) msl_free(p);
+        p = nullptr;
+        bytes = 0;
+        if (!check_status(msl_alloc(&p, need), "halo ring allocation")) return nullptr;
+        bytes = need;
+        return p;
+    }
+};
 
 // DM x DA broadcast zips (src/zip_kernels.cu:45-71): a[r][c] = f(r, c, a[r][c], ...).
 template <typename T, typename T2, typename T3, class F> struct ZipMAOp {  // ..., b[r][c], v[r]
@@ -179,6 +230,37 @@ template <typename T> class DM : public DS<T> {
                          "mapStencilMM");
         result.device_written();
     }
+    // The same with a neutral-value functor (src/dm.cpp:615-919; the
+    // examples' jacobi solver, examples/jacobisolver.cpp:127-136): a read of a
+    // cell (row, col) outside the matrix returns nvf(row, col). The functor
+    // is evaluated on the device once per call for the ring of cells within
+    // the stencil size of the matrix (kept in a buffer of this container
+    // between calls); reads farther out return T{}.
+    template <typename T2, typename MapStencilFunctor, typename NeutralValueFunctor,
+              typename std::enable_if<std::is_class<NeutralValueFunctor>::value, int>::type = 0>
+    void mapStencilMM(DM<T2> &result, MapStencilFunctor &f, NeutralValueFunctor &nvf) {
+        if (result.getSize() != this->n || (void *)&result == (void *)this)
+            return throws(detail::IllegalArgumentException());
+        const int r = f.getStencilSize();
+        if (r < 0) return throws(detail::IllegalArgumentException());
+        this->ensure_device();
+        const HaloRing ring{nrow, ncol, r};
+        T *halo = nullptr;
+        if (ring.size() > 0) {
+            halo = (T *)halo_.reserve((size_t)ring.size() * sizeof(T));
+            if (!halo) return;
+            const int threads = 256;
+            long long blocks = (ring.size() + threads - 1) / threads;
+            if (blocks > 4LL * sm_count()) blocks = 4LL * sm_count();
+            detail::halo_ring_kernel<<<(unsigned)blocks, threads, 0, stream()>>>(halo, ring, nvf);
+            detail::launched(cudaGetLastError(), "mapStencilMM neutral values");
+        }
+        detail::launched(gpu::launch_stencil2d<T>((const T *)this->d_, (T *)result.getDeviceData(), nrow, ncol, r,
+                                                  T{}, detail::PlmNvfCall<T, MapStencilFunctor>{f, halo, r}, nullptr,
+                                                  detail::front_scratch().err, stream()),
+                         "mapStencilMM");
+        result.device_written();
+    }
 
     // ---- row / column skeletons ----
     // c[r] = fold of row r with f, in the GPU build's row-fold order
@@ -298,6 +380,7 @@ template <typename T> class DM : public DS<T> {
 
    private:
     int nrow = 0, ncol = 0;
+    detail::HaloBuffer halo_;
 
     // Rotation into a fresh device buffer, which then replaces the partition.
     void permute(int a, bool rows) {

@@ -74,6 +74,9 @@ template <typename T, typename R> class DMMapStencilFunctor : public detail::Mat
     int stencil_size;
     bool shared_memory = false;
 };
+// Base of stencil functors used with a neutral-value functor
+// (DM::mapStencilMM(result, f, nvf)); the neutral-value functor type is named
+// here only as in the reference, the call passes the object itself.
 template <typename T, typename R, typename NeutralValueFunctor>
 class DMNVFMapStencilFunctor : public DMMapStencilFunctor<T, R> {};
 template <typename T, typename R, typename NeutralValueFunctor>

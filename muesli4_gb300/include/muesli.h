@@ -16,16 +16,25 @@
 
 #include <cuda_runtime.h>
 
+// The standard headers the reference's muesli.h provides to the programs
+// that include it (include/muesli.h:40-58).
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <iostream>
+#include <limits>
+#include <random>
+#include <sstream>
 #include <string>
 #include <vector>
 
 #include "msl_gb300.h"
+#include "msl_single_rank_mpi.h"
 
 #define MSL_USERFUNC __host__ __device__
 #define MSL_GPUFUNC __device__

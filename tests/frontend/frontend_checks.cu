@@ -186,6 +186,35 @@ class GoL : public DMMapStencilFunctor<int, int> {
     }
 };
 
+// mapStencilMM with a neutral-value functor, written like the reference's
+// Jacobi solver (examples/jacobisolver.cpp:15-63): the neutral functor takes
+// (row, col) of a cell outside the matrix; neither functor is symmetric, so
+// the argument order and the halo cells' coordinates are pinned.
+class EdgeValues : public Functor2<int, int, float> {
+   public:
+    EdgeValues(int rows, int cols) : rows_(rows), cols_(cols) {}
+    MSL_USERFUNC float operator()(int row, int col) const override {
+        if (row >= 0 && row < rows_ && col >= 0 && col < cols_) return -1.0f;  // never read
+        return 3.0f * row - 7.0f * col + 0.25f;
+    }
+
+   private:
+    int rows_, cols_;
+};
+class WeightedCross : public DMNVFMapStencilFunctor<float, float, EdgeValues> {
+   public:
+    WeightedCross() : DMNVFMapStencilFunctor() {}
+    MSL_USERFUNC float operator()(int row, int col, PLMatrix<float> *in, int ncol, int nrow) const {
+        const int r = stencil_size;
+        float sum = 0;
+        sum += in->get(row - r, col);
+        sum += 2 * in->get(row + r, col);
+        sum += 4 * in->get(row, col - r);
+        sum += 8 * in->get(row, col + r);
+        return sum / (4 * r);
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -380,6 +409,20 @@ int fe_life_mm(const int *board, int rows, int cols, int iters, int *out) {
         else b.mapStencilMM(a, gol, 0);
     }
     std::memcpy(out, (iters % 2 ? b : a).gather(), sizeof(int) * rows * cols);
+    return 0;
+}
+
+int fe_stencil_mm_nvf(const float *grid, int rows, int cols, int radius, int iters, float *out) {
+    DM<float> a(rows, cols, 0.0f, true), b(rows, cols, 0.0f, true);
+    a.setLocalPartition(const_cast<float *>(grid));
+    EdgeValues edges(rows, cols);
+    WeightedCross f;
+    f.setStencilSize(radius);
+    for (int i = 0; i < iters; i++) {
+        if (i % 2 == 0) a.mapStencilMM(b, f, edges);
+        else b.mapStencilMM(a, f, edges);
+    }
+    std::memcpy(out, (iters % 2 ? b : a).gather(), sizeof(float) * rows * cols);
     return 0;
 }
 

@@ -1,6 +1,6 @@
-// The reference-style program of INTEGRATION.md section 2, verbatim apart from
-// this comment: it must compile and link against the front end and
-// libmsl_gb300.so with the command given there.
+// A reference-style program written against the front end: it must compile
+// and link against the front-end headers and libmsl_gb300.so with the
+// documented nvcc command line.
 #include "muesli.h"
 #include "dm.h"
 using namespace msl;

@@ -113,6 +113,35 @@ def test_life_through_legacy_mapstencilmm(fe, shape, iters):
     assert np.array_equal(out, O.stencil2d_iterate(4, b, 1, 0, iters)[0])
 
 
+def nvf_cross_restated(g, r, iters):
+    """The WeightedCross stencil of frontend_checks.cu over a matrix whose
+    outside cells (row, col) read 3*row - 7*col + 0.25, in float32 with the
+    functor's order of operations (power-of-two weights and divisor: exact)."""
+    rows, cols = g.shape
+    rr, cc = np.meshgrid(np.arange(-r, rows + r), np.arange(-r, cols + r), indexing="ij")
+    halo = (np.float32(3) * rr.astype(np.float32) - np.float32(7) * cc.astype(np.float32)
+            + np.float32(0.25)).astype(np.float32)
+    a = g.astype(np.float32)
+    for _ in range(iters):
+        p = halo.copy()
+        p[r:r + rows, r:r + cols] = a
+        s = np.zeros_like(a)
+        s = s + p[0:rows, r:r + cols]
+        s = s + np.float32(2) * p[2 * r:2 * r + rows, r:r + cols]
+        s = s + np.float32(4) * p[r:r + rows, 0:cols]
+        s = s + np.float32(8) * p[r:r + rows, 2 * r:2 * r + cols]
+        a = (s / np.float32(4 * r)).astype(np.float32)
+    return a
+
+
+@pytest.mark.parametrize("shape,r,iters", [((40, 72), 1, 5), ((97, 33), 2, 4), ((64, 64), 1, 1), ((5, 3), 3, 2)])
+def test_mapstencilmm_with_neutral_value_functor(fe, shape, r, iters):
+    g = W.uniform_f32(shape[0] * shape[1], 0, 100, 21).reshape(shape)
+    out = np.empty_like(g)
+    assert fe.fe_stencil_mm_nvf(ptr(g), shape[0], shape[1], r, iters, ptr(out)) == 0
+    assert np.array_equal(out, nvf_cross_restated(g, r, iters))
+
+
 def test_mapzipfold_lambdas(fe):
     n = (1 << 20) + 3
     x = W.uniform_f32(n, -1, 1, 42)

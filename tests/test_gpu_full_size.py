@@ -41,7 +41,7 @@ def test_da_float_map_zip_fold_2p28(gpu):
     exact = float(np.sum(want_z, dtype=np.float64))
     s_abs = float(np.sum(np.abs(want_z), dtype=np.float64))
     sm, _, _ = gpu.device_info()
-    d = math.ceil(N28 / (sm * 4 * 512)) + 64
+    d = math.ceil(N28 / (sm * 512)) + 64  # at least one 512-thread CTA per SM
     u = 2.0 ** -24
     assert abs(s - exact) <= d * u / (1 - d * u) * s_abs
 

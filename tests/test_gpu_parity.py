@@ -186,7 +186,7 @@ def test_fold_f32_sum_bound(gpu, n):
     got = float(gpu.fold(gpu.MSL_FOLD_SUM, d))
     exact = math.fsum(x.astype(np.float64))
     sm, _, _ = gpu.device_info()
-    threads = sm * 4 * 512
+    threads = sm * 512  # the fold runs at least one 512-thread CTA per SM
     depth = math.ceil(n / threads) + 64
     s_abs = float(np.abs(x.astype(np.float64)).sum())
     assert abs(got - exact) <= gamma(depth) * s_abs + 1e-30
