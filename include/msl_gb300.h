@@ -45,12 +45,16 @@ extern "C" {
 #define MSL_ERR_TIMEOUT (-7)            /* a bounded device-side wait gave up */
 #define MSL_ERR_BUDGET (-8)             /* HBM budget of a batch/server exceeded */
 #define MSL_ERR_UNSUPPORTED_DEVICE (-9) /* FeatureNotSupportedByDeviceException */
+#define MSL_ERR_CANCELLED (-10)         /* a server request cancelled by msl_server_cancel */
 
 /* ---- element types ------------------------------------------------------- */
 #define MSL_F32 0
 #define MSL_F64 1
 #define MSL_I32 2
 #define MSL_BF16 3
+/* batch storage only (msl_batch_create): FP32 solution with bfloat16-stored
+ * corrections, iterated by defect correction */
+#define MSL_BF16_DC 4
 
 /* ---- built-in map functors: out = op(x) ---------------------------------- */
 #define MSL_MAP_AFFINE 0   /* p[0]*x + p[1]  (two roundings, never fused) */
@@ -114,6 +118,26 @@ int msl_set_stream(void *stream);
 int msl_device_info(int *sm_count, size_t *free_bytes, size_t *total_bytes);
 /* Number of kernels this library has launched since msl_init. */
 int msl_launch_count(unsigned long long *count);
+
+/* ---- failure detection ----------------------------------------------------
+ * Every device-side wait of the library's kernels (on an mbarrier that a TMA
+ * copy completes) is bounded: a wait that gives up sets a bit in the
+ * context's device error word, lets its own copy land (a second bounded
+ * wait) and the CTA returns; the next synchronising call returns
+ * MSL_ERR_TIMEOUT and clears the bit, and the context stays usable. None of
+ * this has a reference counterpart: the reference exit()s on CUDA errors
+ * (include/muesli.h:70-77) and never waits on device-side barriers. */
+/* Poll limit of those waits (0 restores the default, about seconds). */
+int msl_set_wait_limit(unsigned polls);
+/* One CTA waits through the same bounded poll (`polls` polls) on a barrier
+ * whose phase completes only if `arrive` is non-zero; returns MSL_OK, or
+ * MSL_ERR_TIMEOUT when the wait gave up. Synchronous. */
+int msl_wait_selftest(unsigned polls, int arrive);
+/* Host-side allocation fault injection: after `after` more allocations by
+ * msl_alloc, msl_batch_create or a server's admission, every further one
+ * fails with MSL_ERR_OUT_OF_MEMORY (checked before anything else, so it works
+ * without a device); a negative value turns the injection off. */
+int msl_debug_fail_allocs(long long after);
 
 /* ---- partition storage (DS<T>) ------------------------------------------- */
 /* Device partition of a container: DS ctor / initGPUs (src/ds.cpp:215-239). */
@@ -282,12 +306,22 @@ int msl_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int 
  * kernel, `depth` fused sweeps per round, the rounds replayed from a CUDA
  * graph. Each grid's sweeps are exactly those of msl_stencil2d_iterate on that
  * grid alone, so results do not depend on the rest of the batch.
- * storage: MSL_F32, or MSL_BF16 (bfloat16 storage, FP32 arithmetic).
+ * storage: MSL_F32, or MSL_BF16 (bfloat16 storage, FP32 arithmetic: the
+ * iterates themselves are bfloat16, so a grid stalls once the updates fall
+ * below half a bfloat16 ulp of its values), or MSL_BF16_DC (defect
+ * correction: the solution u stays FP32; every cycle of check_every sweeps
+ * applies the previous correction, u <- u + d, takes the defect
+ * r = J(u) - u in FP64 -- its max-norm is the residual checked against tol --
+ * and solves d = A d + r, A the Jacobi average of the four neighbours, by
+ * check_every - 1 sweeps over bfloat16-stored d and r from d = r; in exact
+ * arithmetic u + d equals u after check_every Jacobi sweeps. The cycle
+ * (check_every) must be in [2, 64]: the bfloat16 rounding of d accumulates
+ * over a cycle.)
  * hbm_budget (bytes, 0 = none): creation fails with MSL_ERR_BUDGET when the
  * batch would need more device memory. No reference counterpart (the
  * reference solves one DM at a time, examples/jacobisolver.cpp:110-145). */
 int msl_batch_create(int storage, int count, const int *rows, const int *cols, size_t hbm_budget, void **batch);
-/* Set grid `index` from FP32 host values (rounded to bfloat16 for BF16 storage). */
+/* Set grid `index` from FP32 host values (rounded to bfloat16 for MSL_BF16 storage). */
 int msl_batch_set_grid(void *batch, int index, const float *host_grid);
 /* Restore every grid to the values last given by msl_batch_set_grid (device
  * copy) and set its sweep count to 0. */
@@ -298,7 +332,8 @@ int msl_batch_reset(void *batch);
  * a multiple of check_every; check_every must divide max_iters; depth 0 =
  * autotuned. */
 int msl_batch_solve(void *batch, double tol, long long max_iters, int check_every, int depth);
-/* Latest iterate of grid `index` as FP32, with its sweep count and last residual. */
+/* Latest iterate (MSL_BF16_DC: the solution) of grid `index` as FP32, with its
+ * sweep count and last residual. */
 int msl_batch_get_grid(void *batch, int index, float *host_out, long long *iters, double *residual);
 /* Grid count, grids solved CTA-resident, work-list tiles, device bytes (iterates and initial values). */
 int msl_batch_info(void *batch, int *count, int *resident, long long *tiles, size_t *device_bytes);
@@ -328,13 +363,22 @@ int msl_server_start(size_t hbm_budget, double tol, long long max_iters, int che
 /* Queue a request; `init` (FP32 host values) is copied, *request receives its id.
  * A request larger than the whole budget fails with MSL_ERR_BUDGET. */
 int msl_server_submit(void *server, int kind, int depth, int rows, int cols, const float *init, long long *request);
-/* Block until the request finished (timeout_s < 0: no limit; MSL_ERR_TIMEOUT on expiry). */
+/* Block until the request finished (timeout_s < 0: no limit; MSL_ERR_TIMEOUT on
+ * expiry). A request cancelled by msl_server_cancel returns MSL_ERR_CANCELLED;
+ * one whose iterates could not be allocated at admission fails alone with
+ * MSL_ERR_OUT_OF_MEMORY while the others go on. */
 int msl_server_wait(void *server, long long request, double timeout_s);
+/* Cancel a queued or running request: a queued one leaves the queue at once, a
+ * running one is retired (its iterates freed) before the next check interval
+ * and produces no result. The other requests' sweeps and results are not
+ * affected. A request that has already finished cannot be cancelled
+ * (MSL_ERR_INVALID_ARGUMENT). */
+int msl_server_cancel(void *server, long long request);
 /* Result of a finished request: values (FP32, host), sweeps, last residual,
  * latency (submit to completion) and queueing time (submit to admission). */
 int msl_server_result(void *server, long long request, float *out, long long *iters, double *residual,
                       double *latency_s, double *queue_s);
-/* Forget a finished request (frees its host copy of the result). */
+/* Forget a finished, cancelled or out-of-memory request (frees its host copy of the result). */
 int msl_server_release(void *server, long long request);
 int msl_server_stats(void *server, long long *completed, long long *active, long long *queued, size_t *device_bytes,
                      long long *intervals);

@@ -92,6 +92,9 @@ def load() -> ctypes.CDLL:
         "msl_server_stats": [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                              ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(sz), ctypes.POINTER(ctypes.c_longlong)],
         "msl_server_stop": [vp], "msl_server_checkpoint": [vp, ctypes.c_char_p, i],
+        "msl_server_cancel": [vp, ctypes.c_longlong],
+        "msl_set_wait_limit": [ctypes.c_uint], "msl_wait_selftest": [ctypes.c_uint, i],
+        "msl_debug_fail_allocs": [ctypes.c_longlong],
         "msl_server_restore": [ctypes.c_char_p, ctypes.POINTER(vp)],
     }
     for name, args in sig.items():
@@ -290,6 +293,9 @@ class Server:
         check(load().msl_server_result(self.handle, rid, out.ctypes.data, ctypes.byref(it), ctypes.byref(res),
                                        ctypes.byref(lat), ctypes.byref(q)), "msl_server_result")
         return out, it.value, res.value, lat.value, q.value
+
+    def cancel(self, rid: int) -> None:
+        check(load().msl_server_cancel(self.handle, rid), "msl_server_cancel")
 
     def release(self, rid: int) -> None:
         check(load().msl_server_release(self.handle, rid), "msl_server_release")

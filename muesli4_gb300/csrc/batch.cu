@@ -23,7 +23,9 @@ constexpr size_t kResidentSmemMax = 200 * 1024;  // both iterates of a resident 
 
 struct Batch {
     int storage = MSL_F32;
-    size_t es = 4;
+    bool dc = false;   // MSL_BF16_DC: FP32 solution, BF16 corrections (defect correction)
+    size_t es = 4;     // element bytes of the swept arrays (the corrections under defect correction)
+    size_t sol_es = 4; // element bytes of the solution the caller sets and gets
     std::vector<int> rows, cols;
     void *pool = nullptr;
     size_t pool_bytes = 0;
@@ -43,6 +45,7 @@ struct Batch {
 
 void clear_state(BatchGrid &g) {
     g.cur = 0;
+    g.ucur = 0;
     g.done = 0;
     g.iters = 0;
     g.residual = 0.0;
@@ -59,8 +62,15 @@ struct CheckpointGrid {
 static_assert(sizeof(CheckpointGrid) == 32, "checkpoint record layout");
 
 size_t grid_bytes(const Batch &b, int i) { return ((size_t)b.rows[i] * b.cols[i] * b.es + 255) / 256 * 256; }
+size_t sol_bytes(const Batch &b, int i) { return ((size_t)b.rows[i] * b.cols[i] * b.sol_es + 255) / 256 * 256; }
+// Device bytes of one grid: two iterates and the initial values; under defect
+// correction two FP32 solutions, two corrections, the defect and the initial values.
+size_t pool_need(const Batch &b, int i) {
+    return b.dc ? 3 * sol_bytes(b, i) + 3 * grid_bytes(b, i) : 3 * grid_bytes(b, i);
+}
 size_t resident_need(const Batch &b, int i) {
     const size_t n = (size_t)b.rows[i] * b.cols[i];
+    if (b.dc) return (n * 4 + 127) / 128 * 128 + 3 * ((n * 2 + 127) / 128 * 128);
     return 2 * ((n * b.es + 127) / 128 * 128);
 }
 
@@ -177,6 +187,96 @@ int solve_t(Batch &b, double tol, long long max_iters, int check_every, int dept
     return rt::check_device_errors("msl_batch_solve");
 }
 
+// Defect-correction solve: cycles of `cycle` sweeps (see msl_batch.cuh).
+int solve_dc(Batch &b, double tol, long long max_iters, int cycle, int depth) {
+    auto &c = ctx();
+    cudaStream_t st = c.stream;
+    for (auto &g : b.host) {
+        if (g.iters % cycle)
+            return rt::fail(MSL_ERR_INVALID_ARGUMENT,
+                            "msl_batch_solve: a grid stopped after %lld sweeps, not a multiple of the cycle %d", g.iters,
+                            cycle);
+        g.done = g.iters >= max_iters || (g.iters > 0 && !(g.residual > tol));
+        g.resid_bits = 0ull;
+    }
+    // A solve starts without a pending correction: the first step of a grid
+    // re-takes the defect of its solution (the resident kernel clears its own).
+    for (int i : b.worklist)
+        MSL_TRY_CUDA(cudaMemsetAsync(b.host[i].buf[b.host[i].cur], 0, (size_t)b.rows[i] * b.cols[i] * 2, st),
+                     "msl_batch_solve");
+    MSL_TRY_CUDA(cudaMemcpyAsync(b.dev, b.host.data(), b.host.size() * sizeof(BatchGrid), cudaMemcpyHostToDevice, st),
+                 "msl_batch_solve");
+    if (!b.resident.empty()) {
+        MSL_TRY_CUDA(cudaEventRecord(b.fork, st), "msl_batch_solve");
+        MSL_TRY_CUDA(cudaStreamWaitEvent(b.side, b.fork, 0), "msl_batch_solve");
+        auto k = batch_resident_defect_kernel;
+        MSL_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b.resident_smem),
+                     "msl_batch_solve");
+        k<<<(unsigned)b.resident.size(), kBatchResidentThreads, b.resident_smem, b.side>>>(b.dev, b.d_lists, tol,
+                                                                                           max_iters, cycle);
+        MSL_TRY_CUDA(cudaGetLastError(), "msl_batch_solve: resident kernel");
+        rt::count_launch();
+        MSL_TRY_CUDA(cudaEventRecord(b.join, b.side), "msl_batch_solve");
+    }
+    if (!b.worklist.empty()) {
+        const int nlist = (int)b.worklist.size();
+        const int *wl = b.d_lists + b.resident.size();
+        const size_t smem = round_smem<bf16s>(depth);
+        auto rk = batch_round_kernel<bf16s, DefectSel>;
+        if (smem > 48 * 1024)
+            MSL_TRY_CUDA(cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "msl_batch_solve");
+        int per_sm = 1, per_sm_d = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rk, kSt2Threads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_d, batch_defect_kernel, kSt2Threads, 0);
+        auto grid_of = [&](int k) {
+            return (unsigned)std::max(1LL, std::min<long long>(b.total_tiles, (long long)std::max(k, 1) * c.sm_count));
+        };
+        // One cycle: the opening step, then the cycle - 1 correction sweeps in
+        // rounds of `depth` (the last round takes the remainder).
+        std::vector<int> rounds;
+        for (int left = cycle - 1; left > 0; left -= depth) rounds.push_back(std::min(depth, left));
+        const int cycles_per_graph = 4;
+        cudaGraph_t graph;
+        cudaGraphExec_t exec;
+        MSL_TRY_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "msl_batch_solve: capture");
+        for (int j = 0; j < cycles_per_graph; j++) {
+            batch_defect_kernel<<<grid_of(per_sm_d), kSt2Threads, 0, st>>>(b.dev, wl, b.d_tile_grid, b.total_tiles);
+            batch_defect_finalize_kernel<<<1, 256, 0, st>>>(b.dev, wl, nlist, tol, max_iters, b.d_active);
+            for (int d : rounds) {
+                rk<<<grid_of(per_sm), kSt2Threads, smem, st>>>(b.dev, wl, b.d_tile_grid, b.total_tiles, d, 0, nullptr,
+                                                               0, 0.0, 0, nullptr);
+                batch_defect_round_finalize_kernel<<<1, 256, 0, st>>>(b.dev, wl, nlist, d);
+            }
+        }
+        cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        if (ce != cudaSuccess) return rt::cuda_fail(ce, "msl_batch_solve: capture");
+        ce = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return rt::cuda_fail(ce, "msl_batch_solve: instantiate");
+        const long long max_replays = max_iters / ((long long)cycles_per_graph * cycle) + 2;
+        int rc = MSL_OK;
+        for (long long rep = 0; rep < max_replays; rep++) {
+            ce = cudaGraphLaunch(exec, st);
+            if (ce == cudaSuccess) ce = cudaMemcpyAsync(b.h_active, b.d_active, sizeof(int), cudaMemcpyDeviceToHost, st);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+            if (ce != cudaSuccess) {
+                rc = rt::cuda_fail(ce, "msl_batch_solve: cycles");
+                break;
+            }
+            rt::count_launch(cycles_per_graph * 2 * (1 + (int)rounds.size()));
+            if (*(volatile int *)b.h_active == 0) break;
+        }
+        cudaGraphExecDestroy(exec);
+        if (rc != MSL_OK) return rc;
+    }
+    if (!b.resident.empty()) MSL_TRY_CUDA(cudaStreamWaitEvent(st, b.join, 0), "msl_batch_solve");
+    MSL_TRY_CUDA(cudaMemcpyAsync(b.host.data(), b.dev, b.host.size() * sizeof(BatchGrid), cudaMemcpyDeviceToHost, st),
+                 "msl_batch_solve");
+    MSL_TRY_CUDA(cudaStreamSynchronize(st), "msl_batch_solve");
+    return rt::check_device_errors("msl_batch_solve");
+}
+
 }  // namespace
 
 extern "C" {
@@ -184,15 +284,20 @@ extern "C" {
 int msl_batch_create(int storage, int count, const int *rows, const int *cols, size_t hbm_budget, void **batch) {
     auto &c = ctx();
     std::lock_guard<std::recursive_mutex> g(c.mu);
+    if (batch) *batch = nullptr;
+    if (rt::alloc_fault()) return rt::fail(MSL_ERR_OUT_OF_MEMORY, "msl_batch_create: allocation failure injected");
     if (int e = rt::require_init()) return e;
     if (!batch || !rows || !cols || count <= 0)
         return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_create: bad arguments");
-    if (storage != MSL_F32 && storage != MSL_BF16)
-        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_create: storage must be MSL_F32 or MSL_BF16");
+    if (storage != MSL_F32 && storage != MSL_BF16 && storage != MSL_BF16_DC)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT,
+                        "msl_batch_create: storage must be MSL_F32, MSL_BF16 or MSL_BF16_DC");
     *batch = nullptr;
     Batch *b = new Batch;
     b->storage = storage;
-    b->es = rt::dtype_size(storage);
+    b->dc = storage == MSL_BF16_DC;
+    b->es = b->dc ? 2 : rt::dtype_size(storage);
+    b->sol_es = b->dc ? 4 : b->es;
     b->rows.assign(rows, rows + count);
     b->cols.assign(cols, cols + count);
     for (int i = 0; i < count; i++) {
@@ -200,7 +305,7 @@ int msl_batch_create(int storage, int count, const int *rows, const int *cols, s
             destroy(b);
             return rt::fail(MSL_ERR_SIZE_MISMATCH, "msl_batch_create: grid %d is %d x %d", i, rows[i], cols[i]);
         }
-        b->pool_bytes += 3 * grid_bytes(*b, i);
+        b->pool_bytes += pool_need(*b, i);
     }
     const size_t meta = count * sizeof(BatchGrid) + 2 * count * sizeof(int) + 64;
     if (hbm_budget && b->pool_bytes + meta > hbm_budget) {
@@ -232,8 +337,16 @@ int msl_batch_create(int storage, int count, const int *rows, const int *cols, s
         p += grid_bytes(*b, i);
         gd.buf[1] = p;
         p += grid_bytes(*b, i);
+        if (b->dc) {
+            gd.rhs = p;
+            p += grid_bytes(*b, i);
+            gd.u[0] = p;
+            p += sol_bytes(*b, i);
+            gd.u[1] = p;
+            p += sol_bytes(*b, i);
+        }
         b->init[i] = p;
-        p += grid_bytes(*b, i);
+        p += sol_bytes(*b, i);
         if (resident_need(*b, i) <= kResidentSmemMax) {
             b->resident.push_back(i);
             b->resident_smem = std::max(b->resident_smem, resident_need(*b, i));
@@ -286,6 +399,11 @@ int msl_batch_set_grid(void *batch, int index, const float *host_grid) {
     const size_t n = (size_t)b->rows[index] * b->cols[index];
     BatchGrid &gd = b->host[index];
     clear_state(gd);
+    if (b->dc) {
+        MSL_TRY_CUDA(cudaMemcpy(gd.u[0], host_grid, n * 4, cudaMemcpyHostToDevice), "msl_batch_set_grid");
+        MSL_TRY_CUDA(cudaMemcpy(b->init[index], host_grid, n * 4, cudaMemcpyHostToDevice), "msl_batch_set_grid");
+        return MSL_OK;
+    }
     if (b->storage == MSL_F32) {
         MSL_TRY_CUDA(cudaMemcpy(gd.buf[0], host_grid, n * 4, cudaMemcpyHostToDevice), "msl_batch_set_grid");
     } else {
@@ -306,7 +424,9 @@ int msl_batch_get_grid(void *batch, int index, float *host_out, long long *iters
     MSL_TRY_CUDA(cudaStreamSynchronize(c.stream), "msl_batch_get_grid");
     const size_t n = (size_t)b->rows[index] * b->cols[index];
     const BatchGrid &gd = b->host[index];
-    if (b->storage == MSL_F32) {
+    if (b->dc) {
+        MSL_TRY_CUDA(cudaMemcpy(host_out, gd.u[gd.ucur], n * 4, cudaMemcpyDeviceToHost), "msl_batch_get_grid");
+    } else if (b->storage == MSL_F32) {
         MSL_TRY_CUDA(cudaMemcpy(host_out, gd.buf[gd.cur], n * 4, cudaMemcpyDeviceToHost), "msl_batch_get_grid");
     } else {
         std::vector<uint16_t> h(n);
@@ -328,6 +448,15 @@ int msl_batch_solve(void *batch, double tol, long long max_iters, int check_ever
         return rt::fail(MSL_ERR_INVALID_ARGUMENT,
                         "msl_batch_solve: check_every must be >= 1 and divide max_iters (%lld, %d)", max_iters,
                         check_every);
+    if (b->dc) {
+        if (check_every < 2 || check_every > kBatchDefectMaxCycle)
+            return rt::fail(MSL_ERR_INVALID_ARGUMENT,
+                            "msl_batch_solve: the defect-correction cycle (check_every) must be in [2, %d], got %d",
+                            kBatchDefectMaxCycle, check_every);
+        if (depth <= 0) depth = rt::tuned_depth(MSL_BF16, MSL_ST2_JACOBI5, 1024, 1024, 1);
+        if (depth > 8) depth = 8;
+        return solve_dc(*b, tol, max_iters, check_every, depth);
+    }
     if (depth <= 0) depth = rt::tuned_depth(b->storage, MSL_ST2_JACOBI5, 1024, 1024, 1);
     while (depth > 1 && check_every % depth) depth--;
     if (depth > 8) depth = 8;
@@ -342,7 +471,8 @@ int msl_batch_reset(void *batch) {
     if (!b) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_batch_reset: NULL batch");
     for (size_t i = 0; i < b->host.size(); i++) {
         const size_t n = (size_t)b->rows[i] * b->cols[i];
-        MSL_TRY_CUDA(cudaMemcpyAsync(b->host[i].buf[0], b->init[i], n * b->es, cudaMemcpyDeviceToDevice, c.stream),
+        void *dst = b->dc ? b->host[i].u[0] : b->host[i].buf[0];
+        MSL_TRY_CUDA(cudaMemcpyAsync(dst, b->init[i], n * b->sol_es, cudaMemcpyDeviceToDevice, c.stream),
                      "msl_batch_reset");
         clear_state(b->host[i]);
     }
@@ -352,7 +482,8 @@ int msl_batch_reset(void *batch) {
 // Checkpoint file: "MSLBAT01", int32 storage, int32 count, then per grid
 // {int32 rows, int32 cols, int64 sweeps, float64 residual, int32 done,
 // int32 0}, then per grid the latest iterate and the initial values, each
-// rows*cols elements of the storage type. Host byte order.
+// rows*cols elements of the storage type (FP32 under MSL_BF16_DC: the
+// solution; a resumed solve re-takes its defect). Host byte order.
 int msl_batch_checkpoint(void *batch, const char *path) {
     auto &c = ctx();
     std::lock_guard<std::recursive_mutex> g(c.mu);
@@ -371,9 +502,10 @@ int msl_batch_checkpoint(void *batch, const char *path) {
     }
     std::vector<char> h;
     for (size_t i = 0; ok && i < b->host.size(); i++) {
-        const size_t bytes = (size_t)b->rows[i] * b->cols[i] * b->es;
+        const size_t bytes = (size_t)b->rows[i] * b->cols[i] * b->sol_es;
         h.resize(bytes);
-        const void *src[2] = {b->host[i].buf[b->host[i].cur], b->init[i]};
+        const BatchGrid &gd = b->host[i];
+        const void *src[2] = {b->dc ? gd.u[gd.ucur] : gd.buf[gd.cur], b->init[i]};
         for (int k = 0; ok && k < 2; k++) {
             cudaError_t e = cudaMemcpy(h.data(), src[k], bytes, cudaMemcpyDeviceToHost);
             if (e != cudaSuccess) {
@@ -422,9 +554,9 @@ int msl_batch_restore(const char *path, size_t hbm_budget, void **batch) {
     Batch *b = (Batch *)handle;
     std::vector<char> h;
     for (size_t i = 0; ok && i < recs.size(); i++) {
-        const size_t bytes = (size_t)rows[i] * cols[i] * b->es;
+        const size_t bytes = (size_t)rows[i] * cols[i] * b->sol_es;
         h.resize(bytes);
-        void *dst[2] = {b->host[i].buf[0], b->init[i]};
+        void *dst[2] = {b->dc ? b->host[i].u[0] : b->host[i].buf[0], b->init[i]};
         for (int k = 0; ok && k < 2; k++) {
             ok = fread(h.data(), 1, bytes, f) == bytes;
             if (ok && cudaMemcpy(dst[k], h.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) ok = false;

@@ -24,15 +24,23 @@ struct MaxNan {  // max that keeps a NaN (a residual must not hide one)
     __device__ __forceinline__ double operator()(double a, double b) const { return (b > a || b != b) ? b : a; }
 };
 
-// Launch, then copy (value, present) back through the pinned slot.
+// The fold kernel writes (value, present) straight into a mapped pinned
+// host slot (the value at offset 0, the flag at 64): the result reaches the
+// host with the kernel, without a copy after it.
+FoldScratch mapped_result_scratch() {
+    auto &c = ctx();
+    FoldScratch s = c.fold;
+    s.result = c.host_fold_dev;
+    s.result_have = (int *)((char *)c.host_fold_dev + 64);
+    return s;
+}
+
 template <typename R> int finish_fold(void *result, const char *what) {
     auto &c = ctx();
     rt::count_launch();
-    char *h = (char *)c.host_result;
-    MSL_TRY_CUDA(cudaMemcpyAsync(h, c.fold.result, sizeof(R), cudaMemcpyDeviceToHost, c.stream), what);
-    MSL_TRY_CUDA(cudaMemcpyAsync(h + 64, c.fold.result_have, sizeof(int), cudaMemcpyDeviceToHost, c.stream), what);
     MSL_TRY_CUDA(cudaStreamSynchronize(c.stream), what);
-    if (!*(volatile int *)(h + 64)) return rt::fail(MSL_ERR_CUDA, "%s: the fold produced no value", what);
+    const char *h = (const char *)c.host_fold;
+    if (!*(volatile const int *)(h + 64)) return rt::fail(MSL_ERR_CUDA, "%s: the fold produced no value", what);
     memcpy(result, h, sizeof(R));
     return MSL_OK;
 }
@@ -40,7 +48,7 @@ template <typename R> int finish_fold(void *result, const char *what) {
 template <typename T, int OP> int fold_op(const void *in, size_t n, void *result) {
     auto &c = ctx();
     constexpr int V = vec_width1<T>();
-    cudaError_t e = launch_fold<FoldSrcArray, T>(n, FoldOp<T, OP>{}, c.fold, c.stream, c.sm_count,
+    cudaError_t e = launch_fold<FoldSrcArray, T>(n, FoldOp<T, OP>{}, mapped_result_scratch(), c.stream, c.sm_count,
                                                  aligned_to(in, V * sizeof(T)), (const T *)in);
     if (e != cudaSuccess) return rt::cuda_fail(e, "msl_fold");
     return finish_fold<T>(result, "msl_fold");
@@ -59,7 +67,7 @@ template <typename T> int absdiff_t(const void *a, const void *b, size_t n, doub
     auto &c = ctx();
     constexpr int V = vec_width1<T>();
     const bool vec = aligned_to(a, V * sizeof(T)) && aligned_to(b, V * sizeof(T));
-    cudaError_t e = launch_fold<FoldSrcAbsDiff, T>(n, MaxNan{}, c.fold, c.stream, c.sm_count, vec, (const T *)a,
+    cudaError_t e = launch_fold<FoldSrcAbsDiff, T>(n, MaxNan{}, mapped_result_scratch(), c.stream, c.sm_count, vec, (const T *)a,
                                                    (const T *)b);
     if (e != cudaSuccess) return rt::cuda_fail(e, "msl_fold_absdiff_max");
     return finish_fold<double>(result, "msl_fold_absdiff_max");

@@ -27,6 +27,8 @@ struct Context {
     unsigned *err_word = nullptr;      // device error bits (gpu::kErrBarrierTimeout ...)
     unsigned long long *resid = nullptr;  // device residual slot (double bits)
     void *host_result = nullptr;       // pinned host slot for fold/residual results
+    void *host_fold = nullptr;         // mapped pinned slot the fold kernel writes its result to
+    void *host_fold_dev = nullptr;     // its device address
     std::atomic<unsigned long long> launches{0};
     std::recursive_mutex mu;           // serialises the ABI per context
 };
@@ -44,6 +46,11 @@ int check_device_errors(const char *what);
 inline void count_launch(unsigned n = 1) { ctx().launches.fetch_add(n, std::memory_order_relaxed); }
 
 size_t dtype_size(int dtype);
+
+// Host-side allocation fault injection (msl_debug_fail_allocs): true when the
+// allocation about to be made must fail as out of memory. Consumes one
+// allowed allocation otherwise.
+bool alloc_fault();
 
 // Autotuner table (autotune.cu): sweeps per launch recorded for a 2-D stencil
 // of this element type, functor, radius and grid size; 1 when none is recorded.

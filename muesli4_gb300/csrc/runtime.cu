@@ -4,6 +4,7 @@
 // Reference counterparts: msl::initSkeletons / terminateSkeletons /
 // syncStreams (src/muesli.cpp:63-223); DS<T> storage and transfers
 // (src/ds.cpp:215-239, 290-305, 442-591); copyKernel (src/copy_kernel.cu:33-43).
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -70,6 +71,31 @@ size_t dtype_size(int dtype) {
 
 }  // namespace rt
 }  // namespace msl
+
+namespace {
+// Allocations still allowed before injected failures start (-1: no injection).
+std::atomic<long long> g_alloc_allowance{-1};
+
+// One CTA waits on an mbarrier through the library's bounded poll; with
+// `arrive` thread 0 completes the phase first, without it nothing ever does.
+__global__ void wait_selftest_kernel(unsigned *err, unsigned polls, bool arrive) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        msl::gpu::mbar_init(&bar, 1);
+        msl::gpu::fence_barrier_init();
+    }
+    __syncthreads();
+    if (arrive && threadIdx.x == 0) msl::gpu::mbar_arrive(&bar);
+    if (!msl::gpu::mbar_poll(&bar, 0, polls)) msl::gpu::report_error(err, msl::gpu::kErrBarrierTimeout);
+}
+}  // namespace
+
+bool msl::rt::alloc_fault() {
+    long long a = g_alloc_allowance.load();
+    while (a > 0 && !g_alloc_allowance.compare_exchange_weak(a, a - 1)) {
+    }
+    return a == 0;
+}
 
 using namespace msl;
 using msl::rt::ctx;
@@ -144,6 +170,8 @@ int msl_init(int device) {
     c.err_word = (unsigned *)((char *)c.scratch + gpu::kFoldScratchBytes);
     c.resid = (unsigned long long *)((char *)c.scratch + gpu::kFoldScratchBytes + 64);
     MSL_TRY_CUDA(cudaMallocHost(&c.host_result, 256), "msl_init: pinned result slot");
+    MSL_TRY_CUDA(cudaHostAlloc(&c.host_fold, 256, cudaHostAllocMapped), "msl_init: mapped fold slot");
+    MSL_TRY_CUDA(cudaHostGetDevicePointer(&c.host_fold_dev, c.host_fold, 0), "msl_init: mapped fold slot");
     c.device = device;
     c.launches = 0;
     c.initialised = true;
@@ -157,9 +185,11 @@ int msl_terminate(void) {
     cudaStreamSynchronize(c.stream);
     cudaFree(c.scratch);
     cudaFreeHost(c.host_result);
+    cudaFreeHost(c.host_fold);
     cudaStreamDestroy(c.own_stream);
     c.scratch = nullptr;
     c.host_result = nullptr;
+    c.host_fold = c.host_fold_dev = nullptr;
     c.own_stream = c.stream = nullptr;
     c.initialised = false;
     c.device = -1;
@@ -205,6 +235,33 @@ int msl_device_info(int *sm_count, size_t *free_bytes, size_t *total_bytes) {
     return MSL_OK;
 }
 
+int msl_set_wait_limit(unsigned polls) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    if (int e = rt::require_init()) return e;
+    MSL_TRY_CUDA(cudaMemcpyAsync(c.err_word + 1, &polls, sizeof polls, cudaMemcpyHostToDevice, c.stream),
+                 "msl_set_wait_limit");
+    MSL_TRY_CUDA(cudaStreamSynchronize(c.stream), "msl_set_wait_limit");
+    return MSL_OK;
+}
+
+int msl_wait_selftest(unsigned polls, int arrive) {
+    auto &c = ctx();
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    if (int e = rt::require_init()) return e;
+    if (polls == 0) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_wait_selftest: polls must be >= 1");
+    wait_selftest_kernel<<<1, 64, 0, c.stream>>>(c.err_word, polls, arrive != 0);
+    MSL_TRY_CUDA(cudaGetLastError(), "msl_wait_selftest");
+    rt::count_launch();
+    MSL_TRY_CUDA(cudaStreamSynchronize(c.stream), "msl_wait_selftest");
+    return rt::check_device_errors("msl_wait_selftest");
+}
+
+int msl_debug_fail_allocs(long long after) {
+    g_alloc_allowance.store(after < 0 ? -1 : after);
+    return MSL_OK;
+}
+
 int msl_launch_count(unsigned long long *count) {
     if (!count) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_launch_count: NULL");
     *count = ctx().launches.load();
@@ -212,9 +269,11 @@ int msl_launch_count(unsigned long long *count) {
 }
 
 int msl_alloc(void **dptr, size_t bytes) {
-    if (int e = rt::require_init()) return e;
     if (!dptr) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_alloc: NULL result pointer");
     *dptr = nullptr;
+    if (bytes && rt::alloc_fault())
+        return rt::fail(MSL_ERR_OUT_OF_MEMORY, "msl_alloc: %zu bytes: allocation failure injected", bytes);
+    if (int e = rt::require_init()) return e;
     if (bytes == 0) return MSL_OK;
     MSL_TRY_CUDA(cudaMalloc(dptr, bytes), "msl_alloc");
     return MSL_OK;

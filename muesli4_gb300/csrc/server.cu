@@ -45,7 +45,7 @@ using Clock = std::chrono::steady_clock;
 constexpr int kMaxActive = 4096;  // active requests of each kind
 constexpr size_t kResidentSmem = 200 * 1024;  // both iterates of a shared-memory-resident 2-D request
 
-enum ReqState { kQueued = 0, kRunning = 1, kDone = 2, kFailed = 3 };
+enum ReqState { kQueued = 0, kRunning = 1, kDone = 2, kFailed = 3, kCancelled = 4 };
 
 struct Request {
     long long id = 0;
@@ -61,6 +61,9 @@ struct Request {
     int waited = 0;          // consecutive intervals this running request was not scheduled
     int state = kQueued;     // read and written under the server lock
     bool finished = false;   // set by the worker when the request converged or ran out of sweeps
+    bool cancel = false;     // msl_server_cancel on a running request: retired at the next interval boundary
+    int fail_code = 0;       // MSL_ERR_* of a request that failed on its own (kFailed without a server error)
+    std::string fail_why;
     size_t cells() const { return (size_t)depth * rows * cols; }
 };
 
@@ -457,8 +460,11 @@ int write_checkpoint(Server &s, const std::string &path, std::string &why) {
 void worker_loop(Server *sp) {
     Server &s = *sp;
     cudaSetDevice(s.device);
+    std::vector<void *> cancelled_bufs;
     for (;;) {
         std::vector<Request *> act;
+        for (void *p : cancelled_bufs) cudaFreeAsync(p, s.s2);
+        cancelled_bufs.clear();
         {
             std::unique_lock<std::mutex> g(s.mu);
             if (s.ckpt_pending) {  // no work in flight here: every active request sits at an interval end
@@ -470,6 +476,24 @@ void worker_loop(Server *sp) {
                     s.cv_done.notify_all();
                     return;
                 }
+            }
+            // retire running requests cancelled since the last interval (no
+            // device work is in flight here); their iterates are freed below
+            for (size_t i = 0; i < s.active.size();) {
+                Request *r = s.active[i];
+                if (!r->cancel) {
+                    i++;
+                    continue;
+                }
+                r->state = kCancelled;
+                r->t_done = Clock::now();
+                if (r->buf[0]) cancelled_bufs.push_back(r->buf[0]);
+                r->buf[0] = r->buf[1] = nullptr;
+                r->init.clear();
+                r->init.shrink_to_fit();
+                s.used -= r->bytes;
+                s.active.erase(s.active.begin() + i);
+                s.cv_done.notify_all();
             }
             // admit in arrival order while memory and slots allow
             int n2 = 0, n3 = 0;
@@ -496,11 +520,17 @@ void worker_loop(Server *sp) {
         }
         bool ok = true;
         std::string why;
+        std::vector<Request *> no_memory;  // admitted requests whose iterates could not be allocated
         for (Request *r : act) {
             if (r->buf[0]) continue;
             const size_t half = r->bytes / 2;
             void *p = nullptr;
-            cudaError_t e = cudaMallocAsync(&p, r->bytes, s.s2);
+            cudaError_t e = rt::alloc_fault() ? cudaErrorMemoryAllocation : cudaMallocAsync(&p, r->bytes, s.s2);
+            if (e == cudaErrorMemoryAllocation) {  // this request fails alone; the others go on
+                cudaGetLastError();
+                no_memory.push_back(r);
+                continue;
+            }
             if (e == cudaSuccess) {
                 r->buf[0] = p;
                 r->buf[1] = (char *)p + half;
@@ -513,6 +543,20 @@ void worker_loop(Server *sp) {
                 break;
             }
         }
+        if (ok && !no_memory.empty()) {
+            std::lock_guard<std::mutex> g(s.mu);
+            for (Request *r : no_memory) {
+                r->state = kFailed;
+                r->fail_code = MSL_ERR_OUT_OF_MEMORY;
+                r->fail_why = "no device memory for the request's iterates";
+                r->t_done = Clock::now();
+                s.used -= r->bytes;
+                s.active.erase(std::find(s.active.begin(), s.active.end(), r));
+                act.erase(std::find(act.begin(), act.end(), r));
+            }
+            s.cv_done.notify_all();
+        }
+        if (ok && act.empty()) continue;
         if (ok) {
             act = pick_interval(s, act);
             cudaError_t e = run_interval(s, act);
@@ -589,8 +633,8 @@ int msl_server_start(size_t hbm_budget, double tol, long long max_iters, int che
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_res_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_ticket, 2 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(s->d_ticket, 0, 2 * sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_err, sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMemset(s->d_err, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_err, 2 * sizeof(unsigned));  // error word, wait limit (0: default)
+    if (e == cudaSuccess) e = cudaMemset(s->d_err, 0, 2 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_err, sizeof(unsigned));
     if (e == cudaSuccess) *s->h_err = 0;
     if (e == cudaSuccess) e = cudaMalloc(&s->d2, kMaxActive * sizeof(BatchGrid));
@@ -655,10 +699,13 @@ int msl_server_wait(void *server, long long request, double timeout_s) {
     auto it = s->all.find(request);
     if (it == s->all.end()) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_wait: unknown request %lld", request);
     Request *r = it->second.get();
-    auto pred = [&] { return r->state == kDone || r->state == kFailed || s->halted; };
+    auto pred = [&] { return r->state == kDone || r->state == kFailed || r->state == kCancelled || s->halted; };
     if (timeout_s < 0) s->cv_done.wait(g, pred);
     else if (!s->cv_done.wait_for(g, std::chrono::duration<double>(timeout_s), pred))
         return rt::fail(MSL_ERR_TIMEOUT, "msl_server_wait: request %lld not finished", request);
+    if (r->state == kCancelled) return rt::fail(MSL_ERR_CANCELLED, "msl_server_wait: request %lld was cancelled", request);
+    if (r->state == kFailed && r->fail_code)
+        return rt::fail(r->fail_code, "msl_server_wait: request %lld: %s", request, r->fail_why.c_str());
     if (r->state == kFailed) return rt::fail(MSL_ERR_CUDA, "msl_server_wait: %s", s->error.c_str());
     if (r->state != kDone)
         return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_wait: the server halted after a checkpoint");
@@ -673,6 +720,8 @@ int msl_server_result(void *server, long long request, float *out, long long *it
     auto it = s->all.find(request);
     if (it == s->all.end()) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_result: unknown request %lld", request);
     Request *r = it->second.get();
+    if (r->state == kCancelled)
+        return rt::fail(MSL_ERR_CANCELLED, "msl_server_result: request %lld was cancelled", request);
     if (r->state != kDone) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_result: request %lld not done", request);
     if (out) std::memcpy(out, r->out.data(), r->out.size() * sizeof(float));
     if (iters) *iters = r->iters;
@@ -682,12 +731,37 @@ int msl_server_result(void *server, long long request, float *out, long long *it
     return MSL_OK;
 }
 
+int msl_server_cancel(void *server, long long request) {
+    Server *s = as_server(server);
+    if (!s) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_cancel: NULL server");
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->all.find(request);
+    if (it == s->all.end()) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_cancel: unknown request %lld", request);
+    Request *r = it->second.get();
+    if (r->state == kQueued) {
+        s->queue.erase(std::find(s->queue.begin(), s->queue.end(), r));
+        r->state = kCancelled;
+        r->t_done = Clock::now();
+        r->init.clear();
+        r->init.shrink_to_fit();
+        s->cv_done.notify_all();
+        return MSL_OK;
+    }
+    if (r->state == kRunning) {
+        r->cancel = true;  // the worker retires it before its next interval
+        s->cv_work.notify_all();
+        return MSL_OK;
+    }
+    return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_cancel: request %lld has already finished", request);
+}
+
 int msl_server_release(void *server, long long request) {
     Server *s = as_server(server);
     if (!s) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_release: NULL server");
     std::lock_guard<std::mutex> g(s->mu);
     auto it = s->all.find(request);
-    if (it == s->all.end() || it->second->state != kDone)
+    if (it == s->all.end() || (it->second->state != kDone && it->second->state != kCancelled &&
+                               !(it->second->state == kFailed && it->second->fail_code)))
         return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_server_release: request %lld is not a finished request", request);
     s->all.erase(it);
     return MSL_OK;

@@ -25,7 +25,7 @@ namespace msl {
 namespace gpu {
 
 struct BatchGrid {
-    void *buf[2];           // the two iterates (storage type)
+    void *buf[2];           // the two iterates (storage type); defect correction: the two corrections (BF16)
     int rows, cols;
     int cur;                // which buffer holds the latest iterate
     int done;               // converged or out of sweeps
@@ -33,6 +33,11 @@ struct BatchGrid {
     double residual;        // FP64 max |last - previous| at the last check
     unsigned long long resid_bits;  // per-round residual slot (atomic max of double bits)
     long long first_tile;   // prefix of tile counts (work-list grids only)
+    // Defect correction only: the FP32 solution (two buffers, ucur the
+    // latest) and the BF16 defect of the last cycle.
+    void *u[2];
+    void *rhs;
+    int ucur;
 };
 
 // True in every thread of the CTA that finishes last among the launch's CTAs
@@ -96,6 +101,45 @@ struct JacobiFn {
         v = Arith<T>::add(v, m(x, y + 1));
         return Arith<T>::mul(v, T(0.25));
     }
+};
+
+// Defect correction (FP32 solution u, BF16-stored correction d and defect
+// r): a cycle of L sweeps first applies the previous cycle's correction,
+// u <- u + d, and takes the FP64 defect r = J(u) - u of the result (its
+// max-norm is the residual checked against the tolerance); then it solves the
+// correction equation d = A d + r (A: the Jacobi average of the four
+// neighbours, zero on the boundary) by L - 1 sweeps from d = r. In exact
+// arithmetic u + d then equals u after L Jacobi sweeps; the BF16 rounding of
+// d and r is relative to the correction, which shrinks as u converges, so u
+// converges to FP32 accuracy although the sweeps move 16-bit values.
+//
+// The correction sweep: boundary cells stay 0, inside cells take
+// heat5(W, E, N, S) + r, both in FP32.
+struct DefectFn {
+    const bf16s *rhs;
+    int cols;
+    template <class V> __device__ __forceinline__ auto operator()(const V &m, int x, int y) const -> decltype(m(x, y)) {
+        using T = decltype(m(x, y));
+        if (x == 0 || y == 0 || x == m.width - 1 || y == m.height - 1) return T(0);
+        const T v = heat5_value<T>(m(x - 1, y), m(x + 1, y), m(x, y - 1), m(x, y + 1));
+        return Arith<T>::add(v, bf16_to_f(rhs[(size_t)y * cols + x]));
+    }
+};
+// The defect of one inside cell of the corrected solution v (FP32 values):
+// (((W + E) + N) + S) * 0.25 - v in FP64.
+MSL_DEV double defect_f64(float w, float e, float n, float s, float c) {
+    double j = __dadd_rn((double)w, (double)e);
+    j = __dadd_rn(j, (double)n);
+    j = __dadd_rn(j, (double)s);
+    return __dsub_rn(__dmul_rn(j, 0.25), (double)c);
+}
+
+// The functor a round kernel applies to a grid.
+struct JacobiSel {
+    static MSL_DEV JacobiFn make(const BatchGrid &) { return JacobiFn{}; }
+};
+struct DefectSel {
+    static MSL_DEV DefectFn make(const BatchGrid &g) { return DefectFn{(const bf16s *)g.rhs, g.cols}; }
 };
 
 constexpr int kBatchResidentThreads = 512;
@@ -183,7 +227,7 @@ __global__ void __launch_bounds__(kBatchResidentThreads)
 // grids that joined at different times can share a round). Plain coalesced loads
 // stage the windows (grids differ in pointer and shape). `check` marks the
 // round whose last sweep ends a residual-check chunk.
-template <typename S>
+template <typename S, class Sel = JacobiSel>
 __global__ void __launch_bounds__(kSt2Threads)
     batch_round_kernel(BatchGrid *grids, const int *list, const int *tile_grid, long long total_tiles, int depth,
                        int check, unsigned *ticket, int nlist, double tol, long long max_iters, int *active) {
@@ -196,10 +240,10 @@ __global__ void __launch_bounds__(kSt2Threads)
     S *buf0 = reinterpret_cast<S *>(smem_raw + kStHeader);
     S *buf1 = buf0 + buf_elems;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    JacobiFn fn;
     for (long long item = blockIdx.x; item < total_tiles; item += gridDim.x) {
         BatchGrid &g = grids[list[tile_grid[item]]];  // tile_grid: work-list position of the tile's grid
         if (g.done) continue;  // uniform for the CTA
+        const auto fn = Sel::make(g);
         const int rows = g.rows, cols = g.cols;
         const int tiles_x = (cols + kSt2BX - 1) / kSt2BX;
         const unsigned t = (unsigned)(item - g.first_tile);  // < 2^30 cells / 2048 per tile
@@ -245,6 +289,187 @@ __global__ void __launch_bounds__(kSt2Threads)
 static __global__ void batch_finalize_kernel(BatchGrid *grids, const int *list, int nlist, int depth,
                                       int check, double tol, long long max_iters, int *active) {
     batch_finalize_body(grids, list, nlist, depth, check, tol, max_iters, active);
+}
+
+// ---- defect correction ------------------------------------------------------------
+
+// The step that opens a cycle, for every tile of every unfinished work-list
+// grid: v = u + d over the tile and a one-cell halo (FP32), written to the
+// other solution buffer; r = J(v) - v in FP64 for the tile's inside cells,
+// stored as BF16 both as the defect and as the first correction d = r; the
+// tile's max |r| into the grid's residual slot.
+static __global__ void __launch_bounds__(kSt2Threads)
+    batch_defect_kernel(BatchGrid *grids, const int *list, const int *tile_grid, long long total_tiles) {
+    constexpr int hu = 4, hd = 8;  // x halos of the two windows, 16-byte multiples
+    constexpr int pu = kSt2BX + 2 * hu, pd = kSt2BX + 2 * hd, th = kSt2BY + 2;
+    __shared__ __align__(16) float su[th * pu];
+    __shared__ __align__(16) bf16s sd[th * pd];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (long long item = blockIdx.x; item < total_tiles; item += gridDim.x) {
+        BatchGrid &g = grids[list[tile_grid[item]]];
+        if (g.done) continue;
+        const int rows = g.rows, cols = g.cols;
+        const int tiles_x = (cols + kSt2BX - 1) / kSt2BX;
+        const unsigned t = (unsigned)(item - g.first_tile);
+        const int x0 = (int)(t % (unsigned)tiles_x) * kSt2BX, y0 = (int)(t / (unsigned)tiles_x) * kSt2BY;
+        const float *u = (const float *)g.u[g.ucur];
+        float *u_out = (float *)g.u[g.ucur ^ 1];
+        const bf16s *d = (const bf16s *)g.buf[g.cur];
+        bf16s *d_out = (bf16s *)g.buf[g.cur ^ 1];  // neighbouring tiles still read d
+        bf16s *rhs = (bf16s *)g.rhs;
+        __syncthreads();
+        stage_window<float>(su, u, pu, th, th, x0 - hu, y0 - 1, 0, 1, rows, cols);
+        stage_window<bf16s>(sd, d, pd, th, th, x0 - hd, y0 - 1, 0, 1, rows, cols);
+        __syncthreads();
+        for (int k = threadIdx.x; k < th * pu; k += blockDim.x) {  // v = u + d (zero outside the grid)
+            const int yy = k / pu, xx = k - yy * pu;
+            su[k] = __fadd_rn(su[k], bf16_to_f(sd[yy * pd + xx - hu + hd]));
+        }
+        __syncthreads();
+        double dmax = 0.0;
+        const int x = x0 + (warp % (kSt2BX / 32)) * 32 + lane;
+        const int ys = y0 + (warp / (kSt2BX / 32)) * kSt2RPT;
+        if (x < cols) {
+#pragma unroll
+            for (int j = 0; j < kSt2RPT; j++) {
+                const int y = ys + j;
+                if (y >= rows) break;
+                const float *c = su + (y - y0 + 1) * pu + (x - x0 + hu);
+                double dd = 0.0;
+                if (x > 0 && y > 0 && x < cols - 1 && y < rows - 1) {
+                    dd = defect_f64(c[-1], c[1], c[-pu], c[pu], c[0]);
+                    if (fabs(dd) > dmax || dd != dd) dmax = fabs(dd);
+                }
+                const size_t o = (size_t)y * cols + x;
+                const bf16s rb = f_to_bf16(__double2float_rn(dd));
+                u_out[o] = c[0];
+                rhs[o] = rb;
+                d_out[o] = rb;
+            }
+        }
+        dmax = block_max(dmax);
+        if (threadIdx.x == 0) atomic_max_nonneg(&g.resid_bits, dmax);
+    }
+}
+
+// After the cycle-opening step: switch to the corrected solution and check
+// the residual; a grid that goes on counts the sweep that produced d = r.
+static __global__ void batch_defect_finalize_kernel(BatchGrid *grids, const int *list, int nlist, double tol,
+                                                    long long max_iters, int *active) {
+    __shared__ int s_active;
+    if (threadIdx.x == 0) s_active = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nlist; i += blockDim.x) {
+        BatchGrid &g = grids[list[i]];
+        if (g.done) continue;
+        g.ucur ^= 1;
+        g.cur ^= 1;
+        const double r = __longlong_as_double((long long)g.resid_bits);
+        g.residual = r;
+        g.resid_bits = 0ull;
+        if (!(r > tol) || g.iters >= max_iters) g.done = 1;
+        else g.iters += 1;
+        if (!g.done) atomicAdd(&s_active, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *active = s_active;
+}
+// After a correction round of `depth` sweeps.
+static __global__ void batch_defect_round_finalize_kernel(BatchGrid *grids, const int *list, int nlist, int depth) {
+    for (int i = threadIdx.x; i < nlist; i += blockDim.x) {
+        BatchGrid &g = grids[list[i]];
+        if (g.done) continue;
+        g.iters += depth;
+        g.cur ^= 1;
+    }
+}
+
+constexpr int kBatchDefectMaxCycle = 64;
+
+// Resident grids under defect correction: one CTA per grid holds u (FP32),
+// both corrections and the defect (BF16) in shared memory and runs whole
+// cycles until the residual check passes or max_iters sweeps are done; the
+// solution is stored into u[0].
+static __global__ void __launch_bounds__(kBatchResidentThreads)
+    batch_resident_defect_kernel(BatchGrid *grids, const int *list, double tol, long long max_iters, int cycle) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    BatchGrid &g = grids[list[blockIdx.x]];
+    if (g.done) return;
+    const int rows = g.rows, cols = g.cols, n = rows * cols;
+    const int nf = (n * 4 + 127) / 128 * 32, nb = (n * 2 + 127) / 128 * 64;
+    float *su = reinterpret_cast<float *>(smem_raw);
+    bf16s *sd[2] = {reinterpret_cast<bf16s *>(su + nf), reinterpret_cast<bf16s *>(su + nf) + nb};
+    bf16s *sr = sd[1] + nb;
+    const float *ug = (const float *)g.u[g.ucur];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        su[i] = ug[i];
+        sd[0][i] = bf16s{0};  // no pending correction at the start of a solve
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    NPLMatrix<float, bf16s> m;
+    m.width = cols;
+    m.height = rows;
+    m.stencilSize = 1;
+    m.neutralValue = 0.0f;
+    m.global_ = nullptr;
+    m.ox_ = 0;
+    m.oy_ = 0;
+    m.pitch_ = cols;
+    m.tile_h_ = rows;
+    m.check_ = false;  // the functor reads neighbours of inside cells only
+    const DefectFn fn{sr, cols};
+    long long it = g.iters;
+    double res = g.residual;
+    __shared__ int s_stop;
+    for (;;) {
+        // open a cycle: u <- u + d, r = J(u) - u, d = r
+        for (int i = threadIdx.x; i < n; i += blockDim.x) su[i] = __fadd_rn(su[i], bf16_to_f(sd[0][i]));
+        __syncthreads();
+        double dmax = 0.0;
+        for (int y = warp; y < rows; y += nwarps)
+            for (int x = lane; x < cols; x += 32) {
+                const int k = y * cols + x;
+                double dd = 0.0;
+                if (x > 0 && y > 0 && x < cols - 1 && y < rows - 1) {
+                    dd = defect_f64(su[k - 1], su[k + 1], su[k - cols], su[k + cols], su[k]);
+                    if (fabs(dd) > dmax || dd != dd) dmax = fabs(dd);
+                }
+                const bf16s rb = f_to_bf16(__double2float_rn(dd));
+                sr[k] = rb;
+                sd[0][k] = rb;
+            }
+        dmax = block_max(dmax);
+        if (threadIdx.x == 0) {
+            res = dmax;
+            s_stop = !(dmax > tol) || it >= max_iters;
+        }
+        __syncthreads();
+        if (s_stop) break;
+        it += 1;
+        int c = 0;
+        for (int s = 1; s < cycle; s++) {
+            m.tile_ = sd[c];
+            bf16s *dst = sd[c ^ 1];
+            for (int y = warp; y < rows; y += nwarps)
+                for (int x = lane; x < cols; x += 32) dst[y * cols + x] = narrow<bf16s>(fn(m, x, y));
+            __syncthreads();
+            c ^= 1;
+        }
+        it += cycle - 1;
+        if (c) {  // keep the correction in sd[0]
+            for (int i = threadIdx.x; i < n; i += blockDim.x) sd[0][i] = sd[1][i];
+            __syncthreads();
+        }
+    }
+    float *dst_g = (float *)g.u[0];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst_g[i] = su[i];
+    if (threadIdx.x == 0) {
+        g.ucur = 0;
+        g.iters = it;
+        g.residual = res;
+        g.done = 1;
+    }
 }
 
 }  // namespace gpu

@@ -33,6 +33,13 @@ enum : unsigned {
 // Upper bound on mbarrier.try_wait polls (each poll itself blocks for a
 // hardware-defined interval); ~seconds in total, far above any legal wait.
 constexpr unsigned kMaxWaitPolls = 1u << 22;
+// The word after a kernel's error word holds the poll limit of its bounded
+// waits: 0 means kMaxWaitPolls (msl_set_wait_limit sets it for the library's
+// kernels).
+MSL_DEV unsigned wait_poll_limit(const unsigned *err) {
+    const unsigned v = err ? *(volatile const unsigned *)(err + 1) : 0u;
+    return v ? v : kMaxWaitPolls;
+}
 
 MSL_DEV void report_error(unsigned *err, unsigned bits) {
     if (err) atomicOr(err, bits);
@@ -165,6 +172,9 @@ MSL_DEV void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
 }
+MSL_DEV void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 MSL_DEV bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -176,12 +186,21 @@ MSL_DEV bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait for phase `parity` of `bar`; false (and the error bit set) if
-// the phase never completed.
-MSL_DEV bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, unsigned *err) {
-    for (unsigned i = 0; i < kMaxWaitPolls; i++)
+// At most `limit` polls for phase `parity` of `bar`.
+MSL_DEV bool mbar_poll(uint64_t *bar, uint32_t parity, unsigned limit) {
+    for (unsigned i = 0; i < limit; i++)
         if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// Bounded wait for phase `parity` of a barrier that tracks a copy in flight;
+// false (and the error bit set) if the phase did not complete within the
+// poll limit. Before returning false it waits again, up to kMaxWaitPolls
+// polls, for the copy to land, so that a CTA that gives up does not leave a
+// copy writing into shared memory it no longer owns.
+MSL_DEV bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, unsigned *err) {
+    if (mbar_poll(bar, parity, wait_poll_limit(err))) return true;
     report_error(err, kErrBarrierTimeout);
+    mbar_poll(bar, parity, kMaxWaitPolls);
     return false;
 }
 

@@ -158,10 +158,10 @@ __global__ void __launch_bounds__(kFoldThreads, 2)
         if (__ldcg(part_have + k)) fold_in(acc, have, load_cg(partials + k), true, f);
     block_fold(acc, have, f);
     if (threadIdx.x == 0) {
-        *result = acc;
+        *result = acc;  // may be mapped host memory: fenced system-wide
         *result_have = have;
         *ticket = 0u;
-        __threadfence();
+        __threadfence_system();
     }
 }
 

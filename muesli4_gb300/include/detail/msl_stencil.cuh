@@ -608,6 +608,12 @@ __global__ void __launch_bounds__(kSt3Threads, 5)
                 __syncthreads();
             }
             if (!__syncthreads_and(ok)) {
+                if constexpr (TMA) {  // let the plane issued ahead land before the CTA exits
+                    if (threadIdx.x == 0 && z + r + 1 <= ze - 1 + r) {
+                        const int sl = (z + r + 1) & mask;
+                        mbar_poll(&bars[sl], (phase >> sl) & 1u, kMaxWaitPolls);
+                    }
+                }
                 ok = false;
                 break;
             }
@@ -903,7 +909,7 @@ __global__ void __launch_bounds__(kT3Threads, 2)
         bool ok = mbar_wait_bounded(&bar[i & 1], (uint32_t)(i >> 1) & 1u, err);
         ok = __syncthreads_and(ok);
         if (!ok) {  // let the prefetch land before the CTA gives up its shared memory
-            if (threadIdx.x == 0 && nb < nblocks) mbar_wait_bounded(&bar[(i + 1) & 1], (uint32_t)((i + 1) >> 1) & 1u, err);
+            if (threadIdx.x == 0 && nb < nblocks) mbar_poll(&bar[(i + 1) & 1], (uint32_t)((i + 1) >> 1) & 1u, kMaxWaitPolls);
             __syncthreads();
             return;
         }

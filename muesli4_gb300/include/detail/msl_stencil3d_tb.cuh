@@ -111,8 +111,10 @@ __global__ void __launch_bounds__(kT3Threads, 4)
     auto next_in = [](int k) { return k == kZtbIn - 1 ? 0 : k + 1; };
     auto next_mid = [](int k) { return k == kZtbMid - 1 ? 0 : k + 1; };
     auto in_slot = [&](int p) { return (p - zb + 2) % kZtbIn; };  // p >= zb - 2; used outside the loop
+    uint32_t pending = 0;  // thread 0: bit k = a load into slot k not yet waited for
     auto issue = [&](int p) {  // thread 0: TMA load of input plane p (zeros outside the grid)
         const int k = in_slot(p);
+        pending |= 1u << k;
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&bar[k], (uint32_t)(kZtbPlane * sizeof(float)));
         tma_load_3d(in_at(k), &tmap, &bar[k], wx0, wy0, p);
@@ -123,8 +125,9 @@ __global__ void __launch_bounds__(kT3Threads, 4)
     uint32_t phase = 0;  // thread 0: bit k = parity of the next completion of slot k
     auto wait_slot = [&](int k) {
         if (threadIdx.x != 0) return true;
-        const bool ok = mbar_wait_bounded(&bar[k], (phase >> k) & 1u, err);
+        const bool ok = mbar_wait_bounded(&bar[k], (phase >> k) & 1u, err);  // the load has landed either way
         phase ^= 1u << k;
+        pending &= ~(1u << k);
         return ok;
     };
 
@@ -264,7 +267,8 @@ __global__ void __launch_bounds__(kT3Threads, 4)
     }
     if (!ok && threadIdx.x == 0) {
         // let loads still in flight land before the CTA gives up its shared memory
-        for (int k = 0; k < kZtbIn; k++) mbar_wait_bounded(&bar[k], (phase >> k) & 1u, err);
+        for (int k = 0; k < kZtbIn; k++)
+            if (pending & (1u << k)) mbar_poll(&bar[k], (phase >> k) & 1u, kMaxWaitPolls);
     }
     if (want) {
         dmax = block_max(dmax);

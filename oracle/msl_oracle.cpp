@@ -562,6 +562,67 @@ int oracle_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, in
     return 0;
 }
 
+// Plain Jacobi (the sweep functor of examples/jacobisolver.cpp:52-62 on the
+// heatdiffusion operand order, boundary fixed) by defect correction with
+// bfloat16-stored correction d and defect r and an FP32 solution u. The
+// reference has no such solver; this restatement checks the GPU's
+// MSL_BF16_DC batch step for step: each cycle applies u <- u + d, takes
+// r = J(u) - u in FP64 ((((W + E) + N) + S) * 0.25 - u), stops when
+// max |r| <= tol or max_iters sweeps are done, else sets d = r and runs
+// cycle - 1 sweeps d <- heat5(d) + r (FP32, rounded to bfloat16).
+int oracle_jacobi_defect_bf16(float *u, int rows, int cols, double tol, long long max_iters, int cycle,
+                              long long *iters, double *residual) {
+    if (!u || rows <= 0 || cols <= 0 || cycle < 2 || max_iters < 0) return MSL_ERR_INVALID_ARGUMENT;
+    const size_t n = (size_t)rows * cols;
+    std::vector<bf16> d(n, bf16{0}), d2(n, bf16{0}), r(n, bf16{0});
+    auto inside = [&](int x, int y) { return x > 0 && y > 0 && x < cols - 1 && y < rows - 1; };
+    long long it = 0;
+    double res = 0.0;
+    for (;;) {
+        for (size_t k = 0; k < n; k++) u[k] = u[k] + to_f(d[k]);
+        res = 0.0;
+        for (int y = 0; y < rows; y++)
+            for (int x = 0; x < cols; x++) {
+                const size_t k = (size_t)y * cols + x;
+                double dd = 0.0;
+                if (inside(x, y)) {
+                    double j = (double)u[k - 1] + (double)u[k + 1];
+                    j = j + (double)u[k - cols];
+                    j = j + (double)u[k + cols];
+                    dd = j * 0.25 - (double)u[k];
+                    if (std::fabs(dd) > res || dd != dd) res = std::fabs(dd);
+                }
+                r[k] = from_f((float)dd);
+                d[k] = r[k];
+            }
+        if (!(res > tol) || it >= max_iters) break;
+        it += 1;
+        for (int s = 1; s < cycle; s++) {
+            for (int y = 0; y < rows; y++)
+                for (int x = 0; x < cols; x++) {
+                    const size_t k = (size_t)y * cols + x;
+                    if (!inside(x, y)) {
+                        d2[k] = bf16{0};
+                        continue;
+                    }
+                    float v = 0.0f;
+                    v = v + to_f(d[k - 1]);
+                    v = v + to_f(d[k + 1]);
+                    v = v + to_f(d[k - cols]);
+                    v = v + to_f(d[k + cols]);
+                    v = v * 0.25f;
+                    v = v + to_f(r[k]);
+                    d2[k] = from_f(v);
+                }
+            std::swap(d, d2);
+        }
+        it += cycle - 1;
+    }
+    if (iters) *iters = it;
+    if (residual) *residual = res;
+    return 0;
+}
+
 int oracle_stencil3d(int dtype, int kind, const void *in, void *out, int depth, int rows, int cols,
                      int r, double neutral) {
     if (depth <= 0 || rows <= 0 || cols <= 0 || r < 0 || (dtype != MSL_F32 && dtype != MSL_F64) ||

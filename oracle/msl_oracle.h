@@ -40,6 +40,11 @@ int oracle_stencil3d(int dtype, int kind, const void *in, void *out, int depth, 
                      int radius, double neutral);
 int oracle_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int rows, int cols,
                              int radius, double neutral, int iters, double *residual, int *result_in_b);
+/* Plain Jacobi by defect correction with bfloat16-stored correction and
+ * defect (the GPU batch's MSL_BF16_DC mode): u (FP32, in place) is the
+ * solution; returns the sweeps done and the FP64 residual max |J(u) - u|. */
+int oracle_jacobi_defect_bf16(float *u, int rows, int cols, double tol, long long max_iters, int cycle,
+                              long long *iters, double *residual);
 /* DM row / column skeletons: reduceRows (GPU row-fold order), column folds,
  * matrix x per-row-vector zips, rotateRows, rotateCols, setColumn. */
 int oracle_fold_rows(int dtype, int op, const void *in, long long rows, long long cols, int threads_per_block,

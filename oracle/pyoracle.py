@@ -58,6 +58,7 @@ def lib():
         L.oracle_rotate_cols.argtypes = [i, vp, vp, ll, ll, ll]
         L.oracle_set_column.argtypes = [i, vp, vp, ll, ll, ll]
         L.oracle_dump_text.argtypes = [ctypes.c_char_p, i, vp, i, i, i]
+        L.oracle_jacobi_defect_bf16.argtypes = [vp, i, i, d, ll, i, llp, dp]
         _lib = L
     return _lib
 
@@ -175,6 +176,16 @@ def stencil3d_iterate(kind: int, x: np.ndarray, radius: int, neutral: float, ite
                                           float(neutral), iters, ctypes.byref(res), ctypes.byref(inb)),
            "stencil3d_iterate")
     return (b, a, res.value) if inb.value else (a, b, res.value)
+
+
+def jacobi_defect_bf16(x: np.ndarray, tol: float, max_iters: int, cycle: int):
+    """Plain Jacobi by defect correction with bfloat16 corrections: returns
+    (FP32 solution, sweeps, FP64 residual max |J(u) - u|)."""
+    u = np.ascontiguousarray(x, dtype=np.float32).copy()
+    it, res = ctypes.c_longlong(), ctypes.c_double()
+    _check(lib().oracle_jacobi_defect_bf16(_ptr(u), u.shape[0], u.shape[1], float(tol), int(max_iters), int(cycle),
+                                           ctypes.byref(it), ctypes.byref(res)), "jacobi_defect_bf16")
+    return u, it.value, res.value
 
 
 # ---- bfloat16 helpers (storage as uint16) -----------------------------------

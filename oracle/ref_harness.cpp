@@ -213,6 +213,38 @@ int usage() {
 
 }  // namespace
 
+// DM x DA broadcast zips and the DA-with-matrix-rows skeletons (src/dm.cpp:1757-1853,
+// src/dm.cpp:505-535, src/da.cpp:256-324); non-commutative integer functors.
+struct BcMA {  // (r, c, a, b[r][c], u[r])
+    MSL_USERFUNC int operator()(int r, int c, int a, int b, int u) const { return 1000 * r + 7 * c + 2 * a - 3 * b + 5 * u; }
+};
+struct BcA {  // (r, c, a, u[r])
+    MSL_USERFUNC int operator()(int r, int c, int a, int u) const { return 1000 * r + 7 * c - a + 11 * u; }
+};
+struct BcAAA {  // (r, c, a, u[r], v[r], w[r])
+    MSL_USERFUNC int operator()(int r, int c, int a, int u, int v, int w) const {
+        return 1000 * r + 7 * c + a - 2 * u + 3 * v - 5 * w;
+    }
+};
+// crossZipIndexInPlace: a[r][c] <- b[c][r] + a[r][c]. The CPU build calls
+// f(r, c, a[r][c], b_partition) and stores the result (src/dm.cpp:528-532).
+struct BcCross {
+    int n;
+    MSL_USERFUNC int operator()(int r, int c, int a, int *b) const { return b[c * n + r] + a; }
+};
+struct BcRowSum {  // this[i] <- i + sum(row i) - this[i]
+    int cols;
+    MSL_USERFUNC int operator()(int i, int *row, int x) const {
+        int s = 0;
+        for (int k = 0; k < cols; k++) s += row[k];
+        return i + s - x;
+    }
+};
+struct BcRowPick {  // this[i] <- row[i % cols] * b[i] + this[i] + i
+    int cols;
+    MSL_USERFUNC int operator()(int i, int *row, int b, int x) const { return row[i % cols] * b + x + i; }
+};
+
 int main(int argc, char **argv) {
     if (argc < 2) return usage();
     std::string op = argv[1];
@@ -455,6 +487,36 @@ int main(int argc, char **argv) {
         d.setLocalPartition(v.data());
         m.setColumn(d, col);
         store(out, m.getLocalPartition(), n);
+    } else if (op == "dm_zipindex_ma" || op == "dm_zipindex_a" || op == "dm_zipindex_aaa" ||
+               op == "dm_crosszip") {  // rows cols; inputs a, b (rows x cols), u, v, w (rows)
+        int rows = (int)I(0), cols = (int)I(1);
+        size_t n = (size_t)rows * cols;
+        std::vector<int> a = load<int>(ins.at(0), n), b = load<int>(ins.at(1), n);
+        std::vector<int> u = load<int>(ins.at(2), rows), v = load<int>(ins.at(3), rows), w = load<int>(ins.at(4), rows);
+        DM<int> ma(rows, cols, 0, true), mb(rows, cols, 0, true);
+        DA<int> du(rows, 0), dv(rows, 0), dw(rows, 0);
+        ma.setLocalPartition(a.data());
+        mb.setLocalPartition(b.data());
+        du.setLocalPartition(u.data());
+        dv.setLocalPartition(v.data());
+        dw.setLocalPartition(w.data());
+        if (op == "dm_zipindex_ma") { BcMA f; ma.zipIndexInPlaceMA(mb, du, f); }
+        else if (op == "dm_zipindex_a") { BcA f; ma.zipIndexInPlaceA(du, f); }
+        else if (op == "dm_zipindex_aaa") { BcAAA f; ma.zipIndexInPlaceAAA(du, dv, dw, f); }
+        else { BcCross f{cols}; ma.crossZipIndexInPlace(mb, f); }
+        store(out, ma.getLocalPartition(), n);
+    } else if (op == "da_mapindex_dmrows" || op == "da_zipindex_dmrows") {  // rows cols; inputs m, u, v
+        int rows = (int)I(0), cols = (int)I(1);
+        size_t n = (size_t)rows * cols;
+        std::vector<int> a = load<int>(ins.at(0), n), u = load<int>(ins.at(1), rows), v = load<int>(ins.at(2), rows);
+        DM<int> ma(rows, cols, 0, true);
+        DA<int> du(rows, 0), dv(rows, 0);
+        ma.setLocalPartition(a.data());
+        du.setLocalPartition(u.data());
+        dv.setLocalPartition(v.data());
+        if (op == "da_mapindex_dmrows") { BcRowSum f{cols}; du.mapIndexInPlaceDMRows(ma, f); }
+        else { BcRowPick f{cols}; du.zipIndexInPlaceDMRows(dv, ma, f); }
+        store(out, du.getLocalPartition(), rows);
     } else {
         std::fprintf(stderr, "ref_harness: unknown op %s\n", op.c_str());
         return 2;

@@ -149,6 +149,21 @@ def main():
     sv = rng(64).random(17, dtype=np.float32)
     save("dm_set_column", seed=[63, 64], ints=[17, 9, 4], in0=sc, in1=sv,
          out=run("dm_set_column", [17, 9, 4], [sc, sv], np.float32, sc.size))
+
+    # DM x DA broadcast zips and the DA-with-matrix-rows skeletons (int32,
+    # non-commutative functors of oracle/ref_harness.cpp).
+    for tag, (rows, cols) in (("7x5", (7, 5)), ("33x40", (33, 40)), ("16x16", (16, 16))):
+        g = rng(65 + rows)
+        a = g.integers(-1000, 1000, (rows, cols), dtype=np.int32)
+        b = g.integers(-1000, 1000, (rows, cols), dtype=np.int32)
+        u, v, w = (g.integers(-1000, 1000, rows, dtype=np.int32) for _ in range(3))
+        ops = ["dm_zipindex_ma", "dm_zipindex_a", "dm_zipindex_aaa"] + (["dm_crosszip"] if rows == cols else [])
+        for op in ops:
+            save(f"{op}_{tag}", seed=65 + rows, ints=[rows, cols], in0=a, in1=b, in2=u, in3=v, in4=w,
+                 out=run(op, [rows, cols], [a, b, u, v, w], np.int32, a.size))
+        for op in ("da_mapindex_dmrows", "da_zipindex_dmrows"):
+            save(f"{op}_{tag}", seed=65 + rows, ints=[rows, cols], in0=a, in1=u, in2=v,
+                 out=run(op, [rows, cols], [a, u, v], np.int32, rows))
     print("golden fixtures written to", HERE)
 
 

@@ -63,3 +63,33 @@ def test_setters_validate_their_arguments(lib):
     assert lib.msl_set_stencil3d_persistent(2) == bad and lib.msl_set_stencil3d_persistent(-2) == bad
     assert lib.msl_set_stencil3d_persistent(-1) == abi.MSL_OK
     assert lib.msl_set_tma(0) == abi.MSL_OK and lib.msl_set_tma(1) == abi.MSL_OK
+
+
+def test_injected_allocation_failures_need_no_device(lib):
+    """The host-side allocation fault hook: after `after` allowed allocations,
+    msl_alloc and msl_batch_create fail with OUT_OF_MEMORY (checked before the
+    device is needed, so it runs here); -1 turns it off again."""
+    p = ctypes.c_void_p()
+    rows = (ctypes.c_int * 1)(64)
+    h = ctypes.c_void_p()
+    try:
+        assert lib.msl_debug_fail_allocs(0) == abi.MSL_OK
+        assert lib.msl_alloc(ctypes.byref(p), 16) == abi.MSL_ERR_OUT_OF_MEMORY
+        assert b"injected" in lib.msl_last_error_string()
+        assert lib.msl_batch_create(abi.MSL_F32, 1, rows, rows, 0, ctypes.byref(h)) == abi.MSL_ERR_OUT_OF_MEMORY
+        assert not h.value
+        assert lib.msl_debug_fail_allocs(2) == abi.MSL_OK
+        # two allocations pass the hook (and then need the device), the third fails
+        assert lib.msl_alloc(ctypes.byref(p), 16) == abi.MSL_ERR_NOT_INITIALIZED
+        assert lib.msl_batch_create(abi.MSL_F32, 1, rows, rows, 0, ctypes.byref(h)) == abi.MSL_ERR_NOT_INITIALIZED
+        assert lib.msl_alloc(ctypes.byref(p), 16) == abi.MSL_ERR_OUT_OF_MEMORY
+        assert lib.msl_alloc(ctypes.byref(p), 0) == abi.MSL_ERR_NOT_INITIALIZED  # zero bytes allocate nothing
+    finally:
+        lib.msl_debug_fail_allocs(-1)
+    assert lib.msl_alloc(ctypes.byref(p), 16) == abi.MSL_ERR_NOT_INITIALIZED
+
+
+def test_failure_detection_calls_before_init(lib):
+    assert lib.msl_set_wait_limit(4) == abi.MSL_ERR_NOT_INITIALIZED
+    assert lib.msl_wait_selftest(4, 0) == abi.MSL_ERR_NOT_INITIALIZED
+    assert lib.msl_server_cancel(None, 1) == abi.MSL_ERR_INVALID_ARGUMENT

@@ -110,15 +110,93 @@ def test_batch_reset_restores_initial_values(gpu):
     b.close()
 
 
-@pytest.mark.parametrize("storage", ["f32", "bf16"])
+DC_SHAPES = [(48, 64), (64, 64), (33, 200), (150, 200), (257, 333), (96, 700)]
+
+
+@pytest.mark.parametrize("depth", [1, 3, 4])
+def test_defect_correction_batch_matches_oracle(gpu, depth):
+    """MSL_BF16_DC (FP32 solution, bfloat16 corrections) against the CPU
+    restatement of the same defect correction: solution bits, sweep count
+    and FP64 residual, for CTA-resident and work-list grids, at several
+    temporal depths of the correction sweeps (which change nothing)."""
+    tol, max_iters, cycle = 1e-3, 2000, 20
+    grids = [W.jacobi_grid(r, c, 900 + i) for i, (r, c) in enumerate(DC_SHAPES)]
+    batch = gpu.Batch(DC_SHAPES, storage=gpu.MSL_BF16_DC)
+    info = batch.info()
+    assert 0 < info["resident"] < len(DC_SHAPES)
+    for i, g in enumerate(grids):
+        batch.set_grid(i, g)
+    batch.solve(tol, max_iters, cycle, depth)
+    for i, g in enumerate(grids):
+        got, it, res = batch.get_grid(i)
+        want, want_it, want_res = O.jacobi_defect_bf16(g, tol, max_iters, cycle)
+        assert (it, res) == (want_it, want_res), (DC_SHAPES[i], it, want_it, res, want_res)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), DC_SHAPES[i]
+    batch.close()
+
+
+def test_defect_correction_alone_equals_in_the_mix(gpu):
+    tol, max_iters, cycle = 1e-3, 2000, 16
+    shapes = DC_SHAPES[2:]
+    grids = [W.jacobi_grid(r, c, 40 + i) for i, (r, c) in enumerate(shapes)]
+    mix = gpu.Batch(shapes, storage=gpu.MSL_BF16_DC)
+    for i, g in enumerate(grids):
+        mix.set_grid(i, g)
+    mix.solve(tol, max_iters, cycle, 4)
+    for i, g in enumerate(grids):
+        alone = gpu.Batch([shapes[i]], storage=gpu.MSL_BF16_DC)
+        alone.set_grid(0, g)
+        alone.solve(tol, max_iters, cycle, 4)
+        a, ia, ra = alone.get_grid(0)
+        m, im, rm = mix.get_grid(i)
+        assert (ia, ra) == (im, rm) and np.array_equal(a.view(np.uint32), m.view(np.uint32))
+        alone.close()
+    mix.close()
+
+
+def jacobi_defect_f64(u):
+    """max |J(u) - u| over the inside cells, in FP64 on the host."""
+    v = u.astype(np.float64)
+    j = (((v[1:-1, :-2] + v[1:-1, 2:]) + v[:-2, 1:-1]) + v[2:, 1:-1]) * 0.25
+    return float(np.max(np.abs(j - v[1:-1, 1:-1])))
+
+
+# Bound on the defect-correction solution's distance from the FP64 Jacobi
+# iterate after the same number of sweeps: ten times the residual tolerance.
+# Each cycle's correction carries a bfloat16 rounding error relative to the
+# correction itself (2^-9 per stored value); the corrections shrink with the
+# residual, so the accumulated deviation stays a small multiple of tol.
+DC_FP64_BOUND = 10 * 1e-4
+
+
+@pytest.mark.parametrize("shape", [(64, 64), (128, 128), (150, 200)])
+def test_defect_correction_reaches_tolerance_near_fp64(gpu, shape):
+    """A bfloat16-storage solve reaches an FP64 residual <= 1e-4 (checked
+    again on the host from the returned FP32 solution) and stays within
+    DC_FP64_BOUND of the FP64 oracle's Jacobi iterate after the same sweeps."""
+    tol, cycle = 1e-4, 20
+    g = W.jacobi_grid(*shape, 77)
+    batch = gpu.Batch([shape], storage=gpu.MSL_BF16_DC)
+    batch.set_grid(0, g)
+    batch.solve(tol, 400_000, cycle, 4)
+    u, it, res = batch.get_grid(0)
+    batch.close()
+    assert res <= tol and it < 400_000
+    assert jacobi_defect_f64(u) == res
+    ref, _, _ = O.stencil2d_iterate(0, g.astype(np.float64), 1, 0.0, it)
+    err = float(np.max(np.abs(u.astype(np.float64) - ref)))
+    assert err <= DC_FP64_BOUND, err
+
+
+@pytest.mark.parametrize("storage", ["f32", "bf16", "bf16dc"])
 def test_checkpoint_and_resume_equal_one_solve(gpu, storage, tmp_path):
     """Solve 400 sweeps, checkpoint to a file, restore into a new batch and
     continue to 1200: every grid equals one uninterrupted 1200-sweep solve
     (same sweep count, residual and bits). A second solve on the same batch
     continues the same way."""
-    tol, check_every = 1e-4, 100
+    tol, check_every = 1e-4, (20 if storage == "bf16dc" else 100)
     grids = [W.jacobi_grid(r, c, 500 + i) for i, (r, c) in enumerate(SHAPES)]
-    st = gpu.MSL_F32 if storage == "f32" else gpu.MSL_BF16
+    st = {"f32": gpu.MSL_F32, "bf16": gpu.MSL_BF16, "bf16dc": gpu.MSL_BF16_DC}[storage]
     whole = gpu.Batch(SHAPES, storage=st)
     part = gpu.Batch(SHAPES, storage=st)
     for i, g in enumerate(grids):

@@ -246,6 +246,35 @@ def _wrap(a):
     return (np.asarray(a, np.int64) & 0xFFFFFFFF).astype(np.uint32).view(np.int32)
 
 
+BROADCAST_FIXTURES = sorted(os.path.basename(p)[:-4] for pat in ("dm_zipindex_ma_", "dm_zipindex_a_", "dm_zipindex_aaa_",
+                                                                   "dm_crosszip_", "da_mapindex_dmrows_",
+                                                                   "da_zipindex_dmrows_")
+                            for p in glob.glob(os.path.join(HERE, "golden", pat + "*.npz")))
+BROADCAST_KIND = {"dm_zipindex_ma": 0, "dm_zipindex_a": 1, "dm_zipindex_aaa": 2, "dm_crosszip": 3,
+                  "da_mapindex_dmrows": 4, "da_zipindex_dmrows": 5}
+
+
+@pytest.mark.parametrize("name", BROADCAST_FIXTURES)
+def test_dm_da_broadcast_zips_match_reference_fixtures(fe, name):
+    """The front end's broadcast zips against the reference's own outputs
+    (same functors as oracle/ref_harness.cpp; crossZipIndexInPlace in the
+    GPU build's form, which writes through the matrices' pointers)."""
+    f = np.load(os.path.join(HERE, "golden", name + ".npz"))
+    rows, cols = (int(v) for v in f["ints"])
+    kind = BROADCAST_KIND[name.rsplit("_", 1)[0]]
+    a = np.ascontiguousarray(f["in0"].reshape(rows, cols))
+    if kind >= 4:
+        b = np.zeros_like(a)
+        u, v, w = f["in1"].copy(), f["in2"].copy(), np.zeros(rows, np.int32)
+        out = np.empty(rows, np.int32)
+    else:
+        b = np.ascontiguousarray(f["in1"].reshape(rows, cols))
+        u, v, w = f["in2"].copy(), f["in3"].copy(), f["in4"].copy()
+        out = np.empty((rows, cols), np.int32)
+    assert fe.fe_dm_da(kind, ptr(a), ptr(b), ptr(u), ptr(v), ptr(w), rows, cols, ptr(out)) == 0
+    assert np.array_equal(out.ravel(), f["out"]), name
+
+
 @pytest.mark.parametrize("shape", [(1, 1), (7, 5), (64, 64), (33, 1000), (1000, 3)], ids=lambda s: f"{s[0]}x{s[1]}")
 def test_dm_da_broadcast_zips(fe, shape):
     rows, cols = shape

@@ -33,8 +33,43 @@ def load(name):
     return np.load(os.path.join(GOLDEN, name + ".npz"))
 
 
+def wrap32(a):
+    return (np.asarray(a, np.int64) & 0xFFFFFFFF).astype(np.uint32).view(np.int32)
+
+
+BROADCAST = ("dm_zipindex_ma_", "dm_zipindex_aaa_", "dm_zipindex_a_", "dm_crosszip_", "da_mapindex_dmrows_",
+             "da_zipindex_dmrows_")
+
+
+def broadcast_restated(name, f):
+    """The broadcast-zip fixtures (user functors of oracle/ref_harness.cpp,
+    int32) restated with numpy: the skeletons' loops are element-wise, so
+    the restatement is the functor applied to whole arrays."""
+    rows, cols = (int(v) for v in f["ints"])
+    a = f["in0"].astype(np.int64).reshape(rows, cols)
+    r = np.arange(rows, dtype=np.int64)[:, None]
+    c = np.arange(cols, dtype=np.int64)[None, :]
+    if name.startswith("da_"):
+        u, v = f["in1"].astype(np.int64), f["in2"].astype(np.int64)
+        i = np.arange(rows, dtype=np.int64)
+        if name.startswith("da_mapindex_dmrows_"):
+            return wrap32(i + a.sum(axis=1) - u)
+        return wrap32(a[i, i % cols] * v + u + i)
+    b = f["in1"].astype(np.int64).reshape(rows, cols)
+    u, v, w = (f[k].astype(np.int64)[:, None] for k in ("in2", "in3", "in4"))
+    if name.startswith("dm_zipindex_ma_"):
+        return wrap32(1000 * r + 7 * c + 2 * a - 3 * b + 5 * u)
+    if name.startswith("dm_zipindex_aaa_"):
+        return wrap32(1000 * r + 7 * c + a - 2 * u + 3 * v - 5 * w)
+    if name.startswith("dm_zipindex_a_"):
+        return wrap32(1000 * r + 7 * c - a + 11 * u)
+    return wrap32(b.T + a)  # crossZipIndexInPlace
+
+
 def oracle_for(name, f):
     """Recompute fixture `name` with the oracle; returns the flat result."""
+    if name.startswith(BROADCAST):
+        return broadcast_restated(name, f)
     x = f["in0"]
     y = f["in1"] if "in1" in f else None
     ints = [int(v) for v in f["ints"]]
