@@ -503,6 +503,29 @@ class MapZipFold:
             _, h = self.host_out[k]
             A.check(A.load().msl_download(h.ctypes.data, d[k].ptr, h.nbytes), "msl_download")
 
+    def fold_kernel_rates(self, ev, launches=10):
+        """GB/s of the fold kernel alone: msl_fold returns its value to the
+        host, so its part time above includes the host's wait for the kernel;
+        the same kernel through the asynchronous msl_fold_noalloc, timed with
+        CUDA events on the library stream, shows the device time."""
+        import ctypes
+        A, d = self.A, self.dev
+        res = A.DeviceArray((1,), np.float64)
+        out = {}
+        st = ctypes.c_void_p(A.stream_handle())
+        for key, arr, code in (("fold_f32", d["z"], A.MSL_F32), ("fold_i32", d["y"], A.MSL_I32)):
+            for _ in range(2):
+                A.check(A.load().msl_fold_noalloc(code, A.MSL_FOLD_SUM, arr.ptr, self.n, res.ptr, st))
+            A.sync()
+            e0 = ev.record()
+            for _ in range(launches):
+                A.check(A.load().msl_fold_noalloc(code, A.MSL_FOLD_SUM, arr.ptr, self.n, res.ptr, st))
+            e1 = ev.record()
+            A.sync()
+            t = ev.ms(e0, e1) / 1e3 / launches
+            out[key] = {"us_per_launch": t * 1e6, "GB_per_s": 4 * self.n / t / 1e9}
+        return out
+
     def cpu_sample(self, O, threads, min_seconds: float = 0.0):
         from muesli4_gb300 import workloads as W
         n = 1 << 25
@@ -824,6 +847,9 @@ def run_batch(args, dist: Dist):
         w.__init__(A, count=args.batch_grids or w.count, storage=w.storage,
                    cap=max(w.check_every, cap // w.check_every * w.check_every))
     w.setup()
+    if args.temporal_depth > 0:  # a fixed depth instead of the autotuner's
+        w.depth = args.temporal_depth
+        w.tuned["temporal_depth"] = w.depth
     ev = Events(A)
     # Warm-up: short solves (a tenth of the cap) so that every kernel and the
     # round graph have run before the timed solves.
@@ -854,8 +880,8 @@ def run_batch(args, dist: Dist):
     w.e2e_step()
     A.sync()
     e2e_s = dist.max(time.perf_counter() - t0)
-    plain_s = w.plain_seconds()
-    errs = w.fp64_errors(results)
+    plain_s = w.plain_seconds() if not args.batch_timing_only else float("nan")
+    errs = w.fp64_errors(results) if not args.batch_timing_only else [float("nan")]
     if dist.rank == 0:
         gcups = summ["cell_updates"] / (t_max / args.steps) / 1e9
         plain_rate = solved / plain_s
@@ -902,6 +928,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-cap", type=int, default=0, help="sweep cap of the batch workloads")
     ap.add_argument("--batch-grids", type=int, default=0, help="number of grids of the batch workloads")
+    ap.add_argument("--batch-timing-only", action="store_true",
+                    help="batch workloads: skip the plain path and the FP64 errors (for sweeps of settings)")
     ap.add_argument("--serve-requests", type=int, default=400, help="requests of the serve workload (the full stream: 10000)")
     ap.add_argument("--serve-plain-sample", type=int, default=40)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[0.25, 0.5, 1.0, 2.0])
@@ -994,6 +1022,8 @@ def main():
         if hasattr(w, "result_of") and not np.array_equal(w.result_of(k).download(), h):
             raise RuntimeError(f"end-to-end result of {k} differs from the device result")
 
+    kernel_only = w.fold_kernel_rates(ev) if hasattr(w, "fold_kernel_rates") else None
+
     # ---- roofline of the dominant kernel ----
     peak, peak_kind = measured_peaks()
     dom = max(w.parts, key=lambda k: per_part[k])
@@ -1038,6 +1068,8 @@ def main():
                          "compulsory_bytes_per_launch": p.compulsory_bytes,
                          "compulsory_frac": p.compulsory_bytes / avg_launch_s / 1e9 / peak},
             "parts": parts_out,
+            **({"fold_kernel_only": {k: dict(v, frac=v["GB_per_s"] / peak) for k, v in kernel_only.items()}}
+               if kernel_only else {}),
             "cpu_baseline": cpu,
             "gpu_launches": launches,
             "clocks": clocks,

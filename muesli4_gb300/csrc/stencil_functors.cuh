@@ -38,12 +38,13 @@ template <typename T> struct StHeat5 {
 // Plain Jacobi: boundary cells keep their value, inside cells take heat2D.
 template <typename T> struct StJacobi5 {
     static constexpr bool kStrip2 = true;
+    static constexpr bool kStripAnyTile = true;  // strip() reads the window only and handles the edges
     template <class V> __device__ __forceinline__ T operator()(const V &m, int x, int y) const {
         if (x == 0 || y == 0 || x == m.width - 1 || y == m.height - 1) return m(x, y);
         return heat5<T>(m, x, y);
     }
     template <class V> __device__ __forceinline__ void strip(const V &m, int x, int y0, T (&out)[kSt2RPT]) const {
-        heat5_strip<true>(m, x, y0, out);
+        jacobi_strip_window(m, x, y0, out);
     }
 };
 // Box over (2R+1)^2 cells, summed dx outer / dy inner as the meanblur loop

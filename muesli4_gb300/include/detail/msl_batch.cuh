@@ -88,8 +88,9 @@ MSL_DEV void batch_finalize_body(BatchGrid *grids, const int *list, int nlist, i
 // take (((0 + W) + E) + N) + S times 0.25 (heatdiffusion order; x*0.25 == x/4).
 struct JacobiFn {
     static constexpr bool kStrip2 = true;
+    static constexpr bool kStripAnyTile = true;  // strip() reads the window only and handles the edges
     template <class V, typename T> __device__ __forceinline__ void strip(const V &m, int x, int y0, T (&out)[kSt2RPT]) const {
-        heat5_strip<true>(m, x, y0, out);
+        jacobi_strip_window(m, x, y0, out);
     }
     template <class V> __device__ __forceinline__ auto operator()(const V &m, int x, int y) const -> decltype(m(x, y)) {
         using T = decltype(m(x, y));
@@ -116,6 +117,8 @@ struct JacobiFn {
 // The correction sweep: boundary cells stay 0, inside cells take
 // heat5(W, E, N, S) + r, both in FP32.
 struct DefectFn {
+    static constexpr bool kStrip2 = true;
+    static constexpr bool kStripAnyTile = true;  // strip() reads the window (and r) only and handles the edges
     const bf16s *rhs;
     int cols;
     template <class V> __device__ __forceinline__ auto operator()(const V &m, int x, int y) const -> decltype(m(x, y)) {
@@ -123,6 +126,25 @@ struct DefectFn {
         if (x == 0 || y == 0 || x == m.width - 1 || y == m.height - 1) return T(0);
         const T v = heat5_value<T>(m(x - 1, y), m(x + 1, y), m(x, y - 1), m(x, y + 1));
         return Arith<T>::add(v, bf16_to_f(rhs[(size_t)y * cols + x]));
+    }
+    // kSt2RPT cells of column x from row y0, as operator() computes them.
+    template <class V, typename T> __device__ __forceinline__ void strip(const V &m, int x, int y0, T (&out)[kSt2RPT]) const {
+        const auto *p = m.window_at(x, y0 - 1);
+        const int pitch = m.pitch_;
+        T c[kSt2RPT + 2];
+#pragma unroll
+        for (int k = 0; k < kSt2RPT + 2; k++) c[k] = gpu::widen(p[k * pitch]);
+        const bool xb = x <= 0 || x >= m.width - 1;
+#pragma unroll
+        for (int j = 0; j < kSt2RPT; j++) {
+            const int y = y0 + j;
+            out[j] = T(0);
+            if (!(xb || y <= 0 || y >= m.height - 1)) {
+                const auto *q = p + (j + 1) * pitch;
+                const T v = heat5_value<T>(gpu::widen(q[-1]), gpu::widen(q[1]), c[j], c[j + 2]);
+                out[j] = Arith<T>::add(v, bf16_to_f(rhs[(size_t)y * cols + x]));
+            }
+        }
     }
 };
 // The defect of one inside cell of the corrected solution v (FP32 values):
@@ -273,7 +295,7 @@ __global__ void __launch_bounds__(kSt2Threads)
             m.check_ = false;
             stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, check != 0, dmax);
         } else {
-            m.check_ = true;
+            m.check_ = !has_any_tile_strip<std::remove_cv_t<decltype(fn)>>::value;
             stencil2d_strip<S, false>(fn, m, x, ys, rows, cols, out, check != 0, dmax);
         }
         if (check) {

@@ -37,7 +37,9 @@ constexpr unsigned kMaxWaitPolls = 1u << 22;
 // waits: 0 means kMaxWaitPolls (msl_set_wait_limit sets it for the library's
 // kernels).
 MSL_DEV unsigned wait_poll_limit(const unsigned *err) {
-    const unsigned v = err ? *(volatile const unsigned *)(err + 1) : 0u;
+    // set by the host between launches: read through the read-only cache, so
+    // the CTAs of a launch do not all queue on one L2 line
+    const unsigned v = err ? __ldg(err + 1) : 0u;
     return v ? v : kMaxWaitPolls;
 }
 
@@ -198,7 +200,8 @@ MSL_DEV bool mbar_poll(uint64_t *bar, uint32_t parity, unsigned limit) {
 // polls, for the copy to land, so that a CTA that gives up does not leave a
 // copy writing into shared memory it no longer owns.
 MSL_DEV bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, unsigned *err) {
-    if (mbar_poll(bar, parity, wait_poll_limit(err))) return true;
+    if (mbar_try_wait(bar, parity)) return true;  // the first poll needs no limit
+    if (mbar_poll(bar, parity, wait_poll_limit(err) - 1)) return true;
     report_error(err, kErrBarrierTimeout);
     mbar_poll(bar, parity, kMaxWaitPolls);
     return false;

@@ -221,6 +221,34 @@ MSL_DEV void heat5_strip(const V &m, int x, int y0, T (&out)[kSt2RPT]) {
 // adjacent cells at once (register reuse); others are called per cell.
 template <class F, class = void> struct has_strip2 : std::false_type {};
 template <class F> struct has_strip2<F, decltype((void)F::kStrip2, void())> : std::true_type {};
+// Functors whose strip() reads only the staged window and handles the grid's
+// edges itself (kStripAnyTile): boundary tiles then take the strip path too,
+// with the view's bounds test off. The window must hold finite values
+// wherever it lies outside the grid (staging writes zeros there).
+template <class F, class = void> struct has_any_tile_strip : std::false_type {};
+template <class F>
+struct has_any_tile_strip<F, std::void_t<decltype(F::kStripAnyTile)>> : std::bool_constant<F::kStripAnyTile> {};
+
+// Plain Jacobi for kSt2RPT cells of column x from row y0, read from the
+// window only: every cell takes heat2D of its window neighbours, then cells on
+// the grid's edge keep their value (cells outside the grid get their window
+// value and are never stored). Inside cells read only cells of the grid, so
+// the result is that of the checked path.
+template <class V, typename T> MSL_DEV void jacobi_strip_window(const V &m, int x, int y0, T (&out)[kSt2RPT]) {
+    const auto *p = m.window_at(x, y0 - 1);
+    const int pitch = m.pitch_;
+    T c[kSt2RPT + 2];
+#pragma unroll
+    for (int k = 0; k < kSt2RPT + 2; k++) c[k] = gpu::widen(p[k * pitch]);
+    const bool xb = x <= 0 || x >= m.width - 1;
+#pragma unroll
+    for (int j = 0; j < kSt2RPT; j++) {
+        const auto *q = p + (j + 1) * pitch;
+        const T v = heat5_value<T>(gpu::widen(q[-1]), gpu::widen(q[1]), c[j], c[j + 2]);
+        const int y = y0 + j;
+        out[j] = (xb || y <= 0 || y >= m.height - 1) ? c[j + 1] : v;
+    }
+}
 
 MSL_DEV void atomic_max_nonneg(unsigned long long *slot, double v) {
     atomicMax(slot, (unsigned long long)__double_as_longlong(v));
@@ -310,7 +338,7 @@ MSL_DEV void tb_inner_sweeps(const Fn &fn, NPLMatrix<typename Compute<S>::type, 
                 }
             }
         };
-        if (interior) {
+        if (interior || has_any_tile_strip<Fn>::value) {
             m.check_ = false;
             if constexpr (has_strip2<Fn>::value) {
                 // Whole kSt2RPT-row strips through the functor's strip(): the
@@ -403,7 +431,7 @@ __global__ void __launch_bounds__(kSt2Threads)
         m.check_ = false;
         stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, want, dmax);
     } else {
-        m.check_ = true;
+        m.check_ = !has_any_tile_strip<Fn>::value;
         stencil2d_strip<S, false>(fn, m, x, ys, rows, cols, out, want, dmax);
     }
     if (want) {
@@ -474,7 +502,7 @@ __global__ void __launch_bounds__(kSt2Threads)
         m.check_ = false;
         stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, want, dmax);
     } else {
-        m.check_ = true;
+        m.check_ = !has_any_tile_strip<Fn>::value;
         stencil2d_strip<S, false>(fn, m, x, ys, rows, cols, out, want, dmax);
     }
     if (want) {
