@@ -397,9 +397,12 @@ class Jacobi:
         self.h2d, self.d2h = h.nbytes, h.nbytes + 8
         self.residual = None
         d = getattr(self, "fixed_depth", 0)
+        rows = 32
         if d <= 0:
-            d, _ = A.autotune_stencil2d(A.MSL_ST2_JACOBI5, A.MSL_F32, self.side, self.side, 1, 64)
-        self.tuned = {"temporal_depth": d}
+            d, rows, _ = A.autotune_stencil2d_shape(A.MSL_ST2_JACOBI5, A.MSL_F32, self.side, self.side, 1, 64)
+        tiles = ((self.side + 63) // 64) * ((self.side + rows - 1) // rows)
+        self.tuned = {"temporal_depth": d, "tile": f"64x{rows}" if d > 1 else "64x32 (one sweep per launch)",
+                      "threads_per_cta": rows * 8 if d > 1 else 256, "ctas": tiles}
         p = self.parts["jacobi"]
         p.launches = (self.iters + d - 1) // d
         p.bytes_per_launch = 8 * self.side * self.side * self.iters // p.launches

@@ -280,6 +280,12 @@ int msl_set_stencil3d_depth(int sweeps);
  * `depth` generations per launch on cells packed one bit each (its cells are
  * then all 0 or 1), with identical results. No reference counterpart. */
 int msl_set_temporal_depth(int depth);
+/* Tile height of the temporal-blocking kernel: 16, 32 or 64 rows of 64
+ * columns per CTA (128, 256 or 512 threads), or 0 (default) for the
+ * autotuner's record (32 when none). Results do not depend on it. No
+ * reference counterpart (the reference's tiles are tile_width x tile_width,
+ * include/muesli.h:195). */
+int msl_set_tile_rows(int rows);
 /* out = f(view, x, y) for every cell of a rows x cols grid; `radius` is the
  * stencil size r, `neutral` the value outside the grid. in != out.
  * DM::mapStencil<f> (src/dm.cpp:1535-1591), NPLMatrix (include/nplmatrix.h:56-168). */
@@ -399,11 +405,17 @@ int msl_server_stop(void *server);
 
 /* ---- autotuner -------------------------------------------------------------
  * Times msl_stencil2d_iterate over `iters` sweeps of a rows x cols grid for
- * every temporal depth that fits (1, 2, 3, 4, 6, 8, 12, 16, 24, 32), on scratch grids it
- * allocates and frees, records the fastest for (dtype, kind, radius, grid-size
- * class) and returns it with its rate in cell updates per second. The record
- * is used by later iterate calls when the temporal depth is 0. No reference
- * counterpart (the reference fixes tile width 16, include/muesli.h:195). */
+ * every launch shape that fits -- temporal depth 1, 2, 3, 4, 6, 8, 12, 16, 24
+ * or 32 and, for depths >= 2, tiles of 64 x 16, 64 x 32 or 64 x 64 cells
+ * (128, 256 or 512 threads per CTA) -- on scratch grids it allocates and
+ * frees, records the fastest for (dtype, kind, radius, grid-size class) and
+ * returns it with its rate in cell updates per second. The record is used by
+ * later iterate calls when the temporal depth (tile height) setting is 0. No
+ * reference counterpart (the reference fixes tile width 16,
+ * include/muesli.h:195, and 1024-thread blocks, src/muesli.cpp:103). */
+int msl_autotune_stencil2d_shape(int dtype, int kind, int rows, int cols, int radius, int iters, int *best_depth,
+                                 int *best_tile_rows, double *best_rate);
+/* The same, returning the depth only. */
 int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, int iters, int *best_depth,
                            double *best_rate);
 /* Persist / restore the autotuner's records (plain text, one record per line). */

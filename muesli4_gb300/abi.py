@@ -72,6 +72,7 @@ def load() -> ctypes.CDLL:
         "msl_stencil3d": [i, i, vp, vp, i, i, i, i, d],
         "msl_stencil3d_iterate": [i, i, vp, vp, i, i, i, i, d, i, dp, ip],
         "msl_set_temporal_depth": [i], "msl_autotune_stencil2d": [i, i, i, i, i, i, ip, dp],
+        "msl_set_tile_rows": [i], "msl_autotune_stencil2d_shape": [i, i, i, i, i, i, ip, ip, dp],
         "msl_autotune_save": [ctypes.c_char_p], "msl_autotune_load": [ctypes.c_char_p],
         "msl_fold_noalloc": [i, i, vp, sz, vp, vp],
         "msl_fold_rows": [i, i, vp, ll, ll, i, vp], "msl_fold_cols": [i, i, vp, ll, ll, vp],
@@ -162,6 +163,19 @@ def autotune_stencil2d(kind: int, dtype: int, rows: int, cols: int, radius: int,
     check(load().msl_autotune_stencil2d(dtype, kind, rows, cols, radius, iters, ctypes.byref(d), ctypes.byref(r)),
           "msl_autotune_stencil2d")
     return d.value, r.value
+
+
+def autotune_stencil2d_shape(kind: int, dtype: int, rows: int, cols: int, radius: int, iters: int):
+    """Returns (best temporal depth, best tile rows, cell updates per second)."""
+    d, t, r = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+    check(load().msl_autotune_stencil2d_shape(dtype, kind, rows, cols, radius, iters, ctypes.byref(d), ctypes.byref(t),
+                                              ctypes.byref(r)), "msl_autotune_stencil2d_shape")
+    return d.value, t.value, r.value
+
+
+def set_tile_rows(rows: int) -> None:
+    """Tile height of the temporal-blocking kernel (16, 32, 64; 0 = autotuned)."""
+    check(load().msl_set_tile_rows(int(rows)), "msl_set_tile_rows")
 
 
 def autotune_save(path: str) -> None:

@@ -1,8 +1,10 @@
-// Autotuner for the stencil skeletons: times the candidate temporal depths of
-// msl_stencil2d_iterate on the caller's grid shape and records the fastest per
-// (element type, functor, radius, grid-size class). The reference fixes its
-// tiling statically (tile width 16, include/muesli.h:195; 1024-thread blocks,
-// src/muesli.cpp:103).
+// Autotuner for the stencil skeletons: times the candidate launch shapes of
+// msl_stencil2d_iterate -- temporal depth (sweeps per launch) and, for depths
+// of two and more, the tile height of the temporal-blocking kernel (64 x 16,
+// 64 x 32 or 64 x 64 cells on 128, 256 or 512 threads) -- on the caller's
+// grid shape and records the fastest per (element type, functor, radius,
+// grid-size class). The reference fixes its tiling statically (tile width 16,
+// include/muesli.h:195; 1024-thread blocks, src/muesli.cpp:103).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -10,6 +12,7 @@
 #include <mutex>
 #include <tuple>
 
+#include "../include/detail/msl_stencil.cuh"
 #include "msl_internal.h"
 
 namespace msl {
@@ -19,6 +22,7 @@ namespace {
 using Key = std::tuple<int, int, int, int>;  // dtype, kind, radius, size class
 struct Record {
     int depth;
+    int tile_rows;
     double rate;
 };
 std::mutex g_mu;
@@ -35,6 +39,12 @@ int tuned_depth(int dtype, int kind, int rows, int cols, int radius) {
     std::lock_guard<std::mutex> g(g_mu);
     auto it = table().find(Key{dtype, kind, radius, size_class(rows, cols)});
     return it == table().end() ? 1 : it->second.depth;
+}
+
+int tuned_tile_rows(int dtype, int kind, int rows, int cols, int radius) {
+    std::lock_guard<std::mutex> g(g_mu);
+    auto it = table().find(Key{dtype, kind, radius, size_class(rows, cols)});
+    return it == table().end() ? 32 : it->second.tile_rows;
 }
 
 // Fill a tuning grid with a pseudo-random 0/1 pattern (a valid input for
@@ -66,8 +76,8 @@ using namespace msl;
 
 extern "C" {
 
-int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, int iters, int *best_depth,
-                           double *best_rate) {
+int msl_autotune_stencil2d_shape(int dtype, int kind, int rows, int cols, int radius, int iters, int *best_depth,
+                                 int *best_tile_rows, double *best_rate) {
     auto &c = rt::ctx();
     std::lock_guard<std::recursive_mutex> g(c.mu);
     if (int e = rt::require_init()) return e;
@@ -87,28 +97,37 @@ int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, 
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    int best = 1;
+    int best = 1, best_rows = 32;
     double best_r = 0.0;
     int rc = MSL_OK;
     const int saved = 0;
-    const int candidates[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32};
-    const int ncand = (int)(sizeof candidates / sizeof candidates[0]);
-    double rate[ncand] = {};
-    bool usable[ncand] = {};
-    // Warm every depth up once, then time each three times, interleaved, and
-    // keep each depth's best run (clock ramps and other work on the GPU slow
+    // (depth, tile rows); depth 1 is the one-sweep kernel, whose tiles are fixed
+    struct Cand {
+        int depth, tile_rows;
+    };
+    Cand candidates[1 + 9 * 3];
+    int ncand = 0;
+    candidates[ncand++] = Cand{1, 32};
+    const bool tiles_vary = dtype != MSL_I32;  // Life's fused generations run on the packed kernel's own tiles
+    for (int d : {2, 3, 4, 6, 8, 12, 16, 24, 32})
+        for (int t : {16, 32, 64})
+            if (tiles_vary || t == 32) candidates[ncand++] = Cand{d, t};
+    double rate[1 + 9 * 3] = {};
+    bool usable[1 + 9 * 3] = {};
+    // Warm every shape up once, then time each three times, interleaved, and
+    // keep each shape's best run (clock ramps and other work on the GPU slow
     // single runs down, never speed them up).
     for (int round = 0; round < 4 && rc == MSL_OK; round++) {
         for (int k = 0; k < ncand; k++) {
-            const int d = candidates[k];
+            const int d = candidates[k].depth;
             if (d > iters || (round > 0 && !usable[k])) continue;
-            if (msl_set_temporal_depth(d) != MSL_OK) continue;
+            if (msl_set_temporal_depth(d) != MSL_OK || msl_set_tile_rows(candidates[k].tile_rows) != MSL_OK) continue;
             int inb = 0;
             if (round == 0) {
                 rc = msl_stencil2d_iterate(dtype, kind, a, b, rows, cols, radius, 0.0, d, nullptr, &inb);
                 if (rc != MSL_OK) {
                     if (d == 1) break;  // the functor itself is not available: report it
-                    rc = MSL_OK;        // this depth does not fit: skip it
+                    rc = MSL_OK;        // this shape does not fit: skip it
                     continue;
                 }
                 usable[k] = true;
@@ -127,9 +146,11 @@ int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, 
     for (int k = 0; k < ncand; k++)
         if (usable[k] && rate[k] > best_r) {
             best_r = rate[k];
-            best = candidates[k];
+            best = candidates[k].depth;
+            best_rows = candidates[k].tile_rows;
         }
     msl_set_temporal_depth(saved);
+    msl_set_tile_rows(0);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(a);
@@ -137,11 +158,17 @@ int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, 
     if (rc != MSL_OK) return rc;
     {
         std::lock_guard<std::mutex> g2(rt::g_mu);
-        rt::table()[rt::Key{dtype, kind, radius, rt::size_class(rows, cols)}] = rt::Record{best, best_r};
+        rt::table()[rt::Key{dtype, kind, radius, rt::size_class(rows, cols)}] = rt::Record{best, best_rows, best_r};
     }
     if (best_depth) *best_depth = best;
+    if (best_tile_rows) *best_tile_rows = best_rows;
     if (best_rate) *best_rate = best_r;
     return rt::check_device_errors("msl_autotune_stencil2d");
+}
+
+int msl_autotune_stencil2d(int dtype, int kind, int rows, int cols, int radius, int iters, int *best_depth,
+                           double *best_rate) {
+    return msl_autotune_stencil2d_shape(dtype, kind, rows, cols, radius, iters, best_depth, nullptr, best_rate);
 }
 
 int msl_autotune_save(const char *path) {
@@ -149,10 +176,11 @@ int msl_autotune_save(const char *path) {
     FILE *f = std::fopen(path, "w");
     if (!f) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_autotune_save: cannot open %s", path);
     std::lock_guard<std::mutex> g(rt::g_mu);
-    std::fprintf(f, "# dtype kind radius size_class depth rate\n");
+    std::fprintf(f, "# dtype kind radius size_class depth rate tile_rows\n");
     for (auto &kv : rt::table())
-        std::fprintf(f, "%d %d %d %d %d %.6g\n", std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
-                     std::get<3>(kv.first), kv.second.depth, kv.second.rate);
+        std::fprintf(f, "%d %d %d %d %d %.6g %d\n", std::get<0>(kv.first), std::get<1>(kv.first),
+                     std::get<2>(kv.first), std::get<3>(kv.first), kv.second.depth, kv.second.rate,
+                     kv.second.tile_rows);
     std::fclose(f);
     return MSL_OK;
 }
@@ -165,10 +193,11 @@ int msl_autotune_load(const char *path) {
     std::lock_guard<std::mutex> g(rt::g_mu);
     while (std::fgets(line, sizeof line, f)) {
         if (line[0] == '#') continue;
-        int dt, k, r, sc, d;
+        int dt, k, r, sc, d, t = 32;
         double rate;
-        if (std::sscanf(line, "%d %d %d %d %d %lf", &dt, &k, &r, &sc, &d, &rate) == 6 && d >= 1 && d <= 16)
-            rt::table()[rt::Key{dt, k, r, sc}] = rt::Record{d, rate};
+        const int got = std::sscanf(line, "%d %d %d %d %d %lf %d", &dt, &k, &r, &sc, &d, &rate, &t);
+        if (got >= 6 && d >= 1 && d <= 32 && msl::gpu::valid_tile_rows(t))  // no tile height recorded: 32 rows
+            rt::table()[rt::Key{dt, k, r, sc}] = rt::Record{d, t, rate};
     }
     std::fclose(f);
     return MSL_OK;

@@ -55,6 +55,9 @@ bool alloc_fault();
 // Autotuner table (autotune.cu): sweeps per launch recorded for a 2-D stencil
 // of this element type, functor, radius and grid size; 1 when none is recorded.
 int tuned_depth(int dtype, int kind, int rows, int cols, int radius);
+// Tile height (16, 32 or 64 rows of 64 columns) recorded with that depth; 32
+// when none is recorded.
+int tuned_tile_rows(int dtype, int kind, int rows, int cols, int radius);
 
 }  // namespace rt
 }  // namespace msl

@@ -283,12 +283,13 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
             Request *r = big2[k];
             BatchGrid *dg = s.d2 + nw + nres + (int)k;
             const int depth = rt::tuned_depth(MSL_F32, MSL_ST2_JACOBI5, r->rows, r->cols, 1);
+            const int tile_rows = rt::tuned_tile_rows(MSL_F32, MSL_ST2_JACOBI5, r->rows, r->cols, 1);
             float *p = (float *)r->buf[r->cur], *q = (float *)r->buf[r->cur ^ 1];
             for (int i = 0; i < s.check_every;) {
                 const int d = std::min(std::max(depth, 1), s.check_every - i);
                 unsigned long long *resid = i + d == s.check_every ? &dg->resid_bits : nullptr;
                 cudaError_t e = d > 1 ? launch_stencil2d_tb<float>(p, q, r->rows, r->cols, 1, d, 0.0f, JacobiFn{}, resid,
-                                                                   s.d_err, s.s2)
+                                                                   s.d_err, s.s2, true, tile_rows)
                                       : launch_stencil2d<float>(p, q, r->rows, r->cols, 1, 0.0f, JacobiFn{}, resid,
                                                                 s.d_err, s.s2);
                 SERVE_TRY(e);

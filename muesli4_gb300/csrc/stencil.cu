@@ -179,6 +179,15 @@ int iterate(const char *what, void *a, void *b, int iters, int depth, double *re
 }
 
 std::atomic<int> g_temporal_depth{0};
+std::atomic<int> g_tile_rows{0};
+
+// Tile height of the temporal-blocking kernel: the fixed setting, or (0) the
+// autotuner's record, else 32.
+int tile_rows_for(int dtype, int kind, int rows, int cols, int r) {
+    const int t = g_tile_rows.load(std::memory_order_relaxed);
+    if (t > 0) return t;
+    return msl::rt::tuned_tile_rows(dtype, kind, rows, cols, r);
+}
 
 // Sweeps per launch for a 2-D iteration: the fixed setting, or (0) the
 // autotuner's choice recorded for this grid, else 1.
@@ -210,6 +219,13 @@ int msl_set_stencil3d_persistent(int mode) {
     return MSL_OK;
 }
 
+int msl_set_tile_rows(int rows) {
+    if (rows != 0 && !valid_tile_rows(rows))
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_set_tile_rows: %d not 0, 16, 32 or 64", rows);
+    g_tile_rows.store(rows);
+    return MSL_OK;
+}
+
 int msl_set_temporal_depth(int depth) {
     if (depth < 0 || depth > 32) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_set_temporal_depth: %d not in 0..32", depth);
     g_temporal_depth.store(depth);
@@ -233,6 +249,7 @@ int msl_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, int c
     if (int e = check2d("msl_stencil2d_iterate", dtype, kind, a, b, rows, cols, radius)) return e;
     if (iters < 1) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_stencil2d_iterate: iters must be >= 1");
     const int depth = depth_for(dtype, kind, rows, cols, radius);
+    const int tile_rows = tile_rows_for(dtype, kind, rows, cols, radius);
     // Life: every launch after the first reads the output of a Life launch,
     // whose cells are all 0 or 1, and may take the bit-packed kernel. The first
     // launch then runs a single generation (the cell-by-cell kernel at full
@@ -242,7 +259,7 @@ int msl_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, int c
                              depth <= builtin::kLifePackedMaxDepth;
     const int first = life_packed ? 1 : 0;
     const bool generic_tb = depth > 1 && (!life_packed || residual);
-    if (generic_tb && stencil2d_tb_smem<double>(radius, depth) > kMaxStencilSmem)
+    if (generic_tb && stencil2d_tb_smem<double>(radius, depth, tile_rows) > kMaxStencilSmem)
         return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_stencil2d_iterate: temporal depth %d too deep for radius %d",
                         depth, radius);
     int launch_no = 0;
@@ -253,7 +270,9 @@ int msl_stencil2d_iterate(int dtype, int kind, void *a, void *b, int rows, int c
                            cudaError_t e = life_packed_2d(p, q, rows, cols, k);
                            if (e != cudaErrorNotSupported) return e;
                        }
-                       if (k > 1) return tb_sweeps_2d(dtype, kind, p, q, rows, cols, radius, k, neutral, sw.resid, sw.tma);
+                       if (k > 1)
+                           return tb_sweeps_2d(dtype, kind, p, q, rows, cols, radius, k, neutral, sw.resid, sw.tma,
+                                               tile_rows);
                        return dispatch2d(dtype, kind, p, q, rows, cols, radius, neutral, sw);
                    },
                    first);

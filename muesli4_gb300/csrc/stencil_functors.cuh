@@ -177,7 +177,7 @@ namespace builtin {
 // `depth` fused sweeps (temporal blocking) of a built-in 2-D stencil; defined
 // in stencil_tb.cu for Jacobi / heat2D (F32, F64, BF16) and Life (I32).
 cudaError_t tb_sweeps_2d(int dtype, int kind, const void *in, void *out, int rows, int cols, int r, int depth,
-                         double neutral, unsigned long long *resid, bool tma);
+                         double neutral, unsigned long long *resid, bool tma, int tile_rows);
 bool tb_supported_2d(int dtype, int kind);
 // `depth` Life generations of an int32 grid whose cells are all 0 or 1, with
 // the dead (0) border, on the packed kernel of msl_life.cuh (stencil_tb.cu);

@@ -314,7 +314,7 @@ MSL_DEV void stencil2d_strip(const Fn &fn, const View &m, int x, int ys, int row
 // block grown by (depth - s) * r on every side into the other buffer, so the
 // last sweep (left to the caller) has all the cells it reads. On return
 // m.tile_ points at the buffer holding sweep depth-1 (buf0 when depth == 1).
-template <typename S, class Fn>
+template <typename S, int BY = kSt2BY, class Fn>
 MSL_DEV void tb_inner_sweeps(const Fn &fn, NPLMatrix<typename Compute<S>::type, S> &m, S *buf0, S *buf1, int x0,
                              int y0, int rows, int cols, int r, int depth, int pitch, int wx0, int wy0) {
     using T = typename Compute<S>::type;
@@ -322,7 +322,7 @@ MSL_DEV void tb_inner_sweeps(const Fn &fn, NPLMatrix<typename Compute<S>::type, 
     S *dst = buf1;
     for (int s = 1; s < depth; s++) {
         const int ext = (depth - s) * r;  // halo the remaining sweeps still need
-        const int W = kSt2BX + 2 * ext, H = kSt2BY + 2 * ext;
+        const int W = kSt2BX + 2 * ext, H = BY + 2 * ext;
         const int gx0 = x0 - ext, gy0 = y0 - ext;
         const bool interior = gx0 - r >= 0 && gy0 - r >= 0 && gx0 + W + r <= cols && gy0 + H + r <= rows;
         // Every cell of the region, one at a time; cells outside the grid are
@@ -448,19 +448,19 @@ __global__ void __launch_bounds__(kSt2Threads)
 // it does between separate launches, so the result is bit-identical to
 // `depth` single sweeps while HBM sees one read and one write per `depth`
 // sweeps.
-template <typename S, class Fn, bool TMA>
-__global__ void __launch_bounds__(kSt2Threads)
+template <typename S, class Fn, bool TMA, int BY = kSt2BY>
+__global__ void __launch_bounds__(BY * 8)
     stencil2d_tb_kernel(const __grid_constant__ CUtensorMap tmap, const S *in, S *out, int rows, int cols, int r,
                         int depth, int hx, typename Compute<S>::type neutral, Fn fn, unsigned long long *resid,
                         unsigned *err) {
     using T = typename Compute<S>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
-    const int pitch = kSt2BX + 2 * hx, th = kSt2BY + 2 * depth * r;
+    const int pitch = kSt2BX + 2 * hx, th = BY + 2 * depth * r;
     const int buf_elems = (pitch * th * (int)sizeof(S) + 127) / 128 * 128 / (int)sizeof(S);
     S *buf0 = reinterpret_cast<S *>(smem_raw + kStHeader);
     S *buf1 = buf0 + buf_elems;
-    const int x0 = blockIdx.x * kSt2BX, y0 = blockIdx.y * kSt2BY;
+    const int x0 = blockIdx.x * kSt2BX, y0 = blockIdx.y * BY;
     const int wx0 = x0 - hx, wy0 = y0 - depth * r;
     bool ok = true;
     if constexpr (TMA) {
@@ -492,10 +492,10 @@ __global__ void __launch_bounds__(kSt2Threads)
     m.pitch_ = pitch;
     m.tile_h_ = th;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    tb_inner_sweeps<S>(fn, m, buf0, buf1, x0, y0, rows, cols, r, depth, pitch, wx0, wy0);
+    tb_inner_sweeps<S, BY>(fn, m, buf0, buf1, x0, y0, rows, cols, r, depth, pitch, wx0, wy0);
     const int x = x0 + (warp % (kSt2BX / 32)) * 32 + lane;
     const int ys = y0 + (warp / (kSt2BX / 32)) * kSt2RPT;
-    const bool interior = x0 - r >= 0 && y0 - r >= 0 && x0 + kSt2BX + r <= cols && y0 + kSt2BY + r <= rows;
+    const bool interior = x0 - r >= 0 && y0 - r >= 0 && x0 + kSt2BX + r <= cols && y0 + BY + r <= rows;
     const bool want = resid != nullptr;
     double dmax = 0.0;
     if (interior) {
@@ -1064,22 +1064,25 @@ cudaError_t launch_stencil2d(const S *in, S *out, int rows, int cols, int r, typ
     return cudaGetLastError();
 }
 
-template <typename S> inline size_t stencil2d_tb_smem(int r, int depth) {
-    const int pitch = kSt2BX + 2 * halo_x<S>(depth * r), th = kSt2BY + 2 * depth * r;
+// Tile heights of the temporal-blocking kernel: 64 x BY outputs per CTA of
+// BY * 8 threads (each thread a kSt2RPT-row strip of one column).
+inline bool valid_tile_rows(int by) { return by == 16 || by == 32 || by == 64; }
+
+template <typename S> inline size_t stencil2d_tb_smem(int r, int depth, int by = kSt2BY) {
+    const int pitch = kSt2BX + 2 * halo_x<S>(depth * r), th = by + 2 * depth * r;
     const size_t buf = ((size_t)pitch * th * sizeof(S) + 127) / 128 * 128;
     return (size_t)kStHeader + 2 * buf;
 }
 
-// `depth` fused sweeps in -> out (depth >= 2; depth 1 is launch_stencil2d).
-template <typename S, class Fn>
-cudaError_t launch_stencil2d_tb(const S *in, S *out, int rows, int cols, int r, int depth,
-                                typename Compute<S>::type neutral, Fn fn, unsigned long long *resid, unsigned *err,
-                                cudaStream_t st, bool allow_tma = true) {
+template <typename S, class Fn, int BY>
+cudaError_t launch_stencil2d_tb_rows(const S *in, S *out, int rows, int cols, int r, int depth,
+                                     typename Compute<S>::type neutral, Fn fn, unsigned long long *resid,
+                                     unsigned *err, cudaStream_t st, bool allow_tma) {
     const int hx = halo_x<S>(depth * r);
-    const int pitch = kSt2BX + 2 * hx, th = kSt2BY + 2 * depth * r;
-    const size_t smem = stencil2d_tb_smem<S>(r, depth);
+    const int pitch = kSt2BX + 2 * hx, th = BY + 2 * depth * r;
+    const size_t smem = stencil2d_tb_smem<S>(r, depth, BY);
     if (smem > kMaxStencilSmem) return cudaErrorInvalidValue;
-    dim3 grid((cols + kSt2BX - 1) / kSt2BX, (rows + kSt2BY - 1) / kSt2BY);
+    dim3 grid((cols + kSt2BX - 1) / kSt2BX, (rows + BY - 1) / BY);
     CUtensorMap map{};
     const bool tma = allow_tma && stencil_tma_ok<S>(in, cols, pitch, th);
     if (tma) {
@@ -1091,15 +1094,34 @@ cudaError_t launch_stencil2d_tb(const S *in, S *out, int rows, int cols, int r, 
                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return cudaErrorInvalidValue;
-        auto k = stencil2d_tb_kernel<S, Fn, true>;
+        auto k = stencil2d_tb_kernel<S, Fn, true, BY>;
         if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, kSt2Threads, smem, st>>>(map, in, out, rows, cols, r, depth, hx, neutral, fn, resid, err);
+        k<<<grid, BY * 8, smem, st>>>(map, in, out, rows, cols, r, depth, hx, neutral, fn, resid, err);
     } else {
-        auto k = stencil2d_tb_kernel<S, Fn, false>;
+        auto k = stencil2d_tb_kernel<S, Fn, false, BY>;
         if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, kSt2Threads, smem, st>>>(map, in, out, rows, cols, r, depth, hx, neutral, fn, resid, err);
+        k<<<grid, BY * 8, smem, st>>>(map, in, out, rows, cols, r, depth, hx, neutral, fn, resid, err);
     }
     return cudaGetLastError();
+}
+
+// `depth` fused sweeps in -> out (depth >= 2; depth 1 is launch_stencil2d), on
+// 64 x tile_rows tiles (16, 32 or 64 rows: 128, 256 or 512 threads per CTA).
+template <typename S, class Fn>
+cudaError_t launch_stencil2d_tb(const S *in, S *out, int rows, int cols, int r, int depth,
+                                typename Compute<S>::type neutral, Fn fn, unsigned long long *resid, unsigned *err,
+                                cudaStream_t st, bool allow_tma = true, int tile_rows = kSt2BY) {
+    switch (tile_rows) {
+        case 16:
+            return launch_stencil2d_tb_rows<S, Fn, 16>(in, out, rows, cols, r, depth, neutral, fn, resid, err, st,
+                                                       allow_tma);
+        case 64:
+            return launch_stencil2d_tb_rows<S, Fn, 64>(in, out, rows, cols, r, depth, neutral, fn, resid, err, st,
+                                                       allow_tma);
+        default:
+            return launch_stencil2d_tb_rows<S, Fn, 32>(in, out, rows, cols, r, depth, neutral, fn, resid, err, st,
+                                                       allow_tma);
+    }
 }
 
 template <typename S> inline size_t stencil3d_tile_smem(int r) {

@@ -93,3 +93,10 @@ def test_failure_detection_calls_before_init(lib):
     assert lib.msl_set_wait_limit(4) == abi.MSL_ERR_NOT_INITIALIZED
     assert lib.msl_wait_selftest(4, 0) == abi.MSL_ERR_NOT_INITIALIZED
     assert lib.msl_server_cancel(None, 1) == abi.MSL_ERR_INVALID_ARGUMENT
+
+
+def test_tile_rows_setter_needs_no_device(lib):
+    bad = abi.MSL_ERR_INVALID_ARGUMENT
+    assert lib.msl_set_tile_rows(24) == bad and lib.msl_set_tile_rows(-1) == bad and lib.msl_set_tile_rows(128) == bad
+    for ok in (16, 32, 64, 0):
+        assert lib.msl_set_tile_rows(ok) == abi.MSL_OK

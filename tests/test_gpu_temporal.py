@@ -17,6 +17,7 @@ pytestmark = pytest.mark.gpu
 def depth(gpu):
     yield gpu.set_temporal_depth
     gpu.set_temporal_depth(0)
+    gpu.set_tile_rows(0)
     gpu.set_tma(True)
 
 
@@ -37,6 +38,38 @@ def test_jacobi_fused_sweeps(gpu, depth, d, shape, tma):
     want, _, want_res = O.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, g, 1, 0.0, iters)
     assert bits_equal(last.download(), want)
     assert res == want_res
+
+
+@pytest.mark.parametrize("rows", [16, 64])
+@pytest.mark.parametrize("d", [2, 5])
+@pytest.mark.parametrize("shape", [(33, 47), (130, 200), (257, 1000)], ids=str)
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+def test_tile_rows_do_not_change_results(gpu, depth, rows, d, shape, dtype):
+    """The 64 x 16 (128 threads) and 64 x 64 (512 threads) tiles of the
+    temporal-blocking kernel give the one-sweep-at-a-time results."""
+    depth(d)
+    gpu.set_tile_rows(rows)
+    g = W.jacobi_grid(*shape, seed=rows + d)
+    if dtype == "bf16":
+        g = O.to_bf16(g)
+    a, b = gpu.DeviceArray.from_host(g), gpu.DeviceArray(g.shape, g.dtype)
+    iters = 3 * d + 1
+    last, res = gpu.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, a, b, 1, 0.0, iters)
+    want, _, want_res = O.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, g, 1, 0.0, iters)
+    assert bits_equal(last.download(), want)
+    assert res == want_res
+    x = np.random.default_rng(d).random(shape, dtype=np.float32)
+    a, b = gpu.DeviceArray.from_host(x), gpu.DeviceArray(x.shape, x.dtype)
+    last, res = gpu.stencil2d_iterate(gpu.MSL_ST2_HEAT5, a, b, 1, 0.75, iters)
+    want, _, want_res = O.stencil2d_iterate(gpu.MSL_ST2_HEAT5, x, 1, 0.75, iters)
+    assert bits_equal(last.download(), want) and res == want_res
+
+
+def test_tile_rows_setting_is_validated(gpu, depth):
+    for bad in (8, 24, 128, -1):
+        with pytest.raises(gpu.MslError) as e:
+            gpu.set_tile_rows(bad)
+        assert e.value.code == gpu.MSL_ERR_INVALID_ARGUMENT
 
 
 @pytest.mark.parametrize("d", [2, 4, 6])
@@ -103,8 +136,11 @@ def test_too_deep_is_an_error(gpu, depth):
 
 
 def test_autotuner_records_and_is_used(gpu, depth, tmp_path):
-    best, rate = gpu.autotune_stencil2d(gpu.MSL_ST2_JACOBI5, gpu.MSL_F32, 1024, 1024, 1, 64)
-    assert best in (1, 2, 3, 4, 6, 8) and rate > 0
+    best, rows, rate = gpu.autotune_stencil2d_shape(gpu.MSL_ST2_JACOBI5, gpu.MSL_F32, 1024, 1024, 1, 64)
+    assert best in (1, 2, 3, 4, 6, 8, 12, 16, 24, 32) and rows in (16, 32, 64) and rate > 0
+    assert best > 1 or rows == 32
+    best2, rate2 = gpu.autotune_stencil2d(gpu.MSL_ST2_JACOBI5, gpu.MSL_F32, 1024, 1024, 1, 64)
+    assert best2 in (1, 2, 3, 4, 6, 8, 12, 16, 24, 32) and rate2 > 0
     path = str(tmp_path / "tune.txt")
     gpu.autotune_save(path)
     gpu.autotune_load(path)
