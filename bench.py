@@ -549,6 +549,11 @@ class MapZipFold:
         return self.bytes() / total_t / 1e9, f"2^25-element arrays ({threads} threads; folds on 1 thread)"
 
 
+def side_class(n):
+    return "64-127" if n < 128 else "128-255" if n < 256 else "256-511" if n < 512 else "512-1023" if n < 1024 \
+        else "1024-2048"
+
+
 class BatchSolve:
     """Batched plain-Jacobi solves: 256 grids, sides log-uniform in [64, 2048]
     rounded to multiples of 32 (seed 7), initialised as the plain-Jacobi grid
@@ -628,8 +633,7 @@ class BatchSolve:
         sweeps = sum(it * n * n for it, n in zip(iters, self.sides))
         by_side = {}
         for n, c in zip(self.sides, conv):
-            k = "64-127" if n < 128 else "128-255" if n < 256 else "256-511" if n < 512 else "512-1023" if n < 1024 \
-                else "1024-2048"
+            k = side_class(n)
             by_side.setdefault(k, [0, 0])
             by_side[k][0] += int(c)
             by_side[k][1] += 1
@@ -645,7 +649,9 @@ class BatchSolve:
         the summed solve time (allocation and upload outside the timing)."""
         A = self.A
         t = 0.0
+        self.plain_by_side = {}
         for g, n in enumerate(self.sides):
+            t_before = t
             if self.storage == "f32":
                 a, b = A.DeviceArray.from_host(self.grids[g]), A.DeviceArray((n, n), np.float32)
                 A.sync()
@@ -663,6 +669,8 @@ class BatchSolve:
                 A.sync()
                 t += time.perf_counter() - t0
                 one.close()
+            k = side_class(n)
+            self.plain_by_side[k] = self.plain_by_side.get(k, 0.0) + (t - t_before)
         return t
 
     def fp64_errors(self, results):
@@ -747,11 +755,12 @@ def serve_requests(count: int, seed: int = 11):
 
 
 def run_serve(args, dist: Dist):
-    """Served stencil solves (Jacobi and heat3D requests of mixed sizes): Poisson arrivals at rates
-    swept around the plain path's capacity; p50/p99 latency and solves/s of the
-    continuously batching server against the one-request-at-a-time GPU path
-    (FIFO queue fed the same arrivals; its service times are measured on a
-    sample of the requests and the queue is replayed from them)."""
+    """Served stencil solves (Jacobi and heat3D requests of mixed sizes): Poisson
+    arrivals at rates swept around the plain path's capacity; p50/p99 latency
+    and solves/s of the continuously batching server against the plain
+    one-request-at-a-time GPU path fed the same arrivals (a FIFO queue served
+    for real in the same process: each request waits for its arrival time and
+    for the requests before it, then runs alone through the stencil skeleton)."""
     from muesli4_gb300 import abi as A
     A.init(dist.local_rank)
     tol, cap, check = 1e-4, 5000, 100
@@ -764,35 +773,39 @@ def run_serve(args, dist: Dist):
             cache[i] = np.random.default_rng(sd).random(shape, dtype=np.float32)
         return cache[i]
 
-    # The autotuner picks the 2-D temporal depth per grid-size class; the plain
+    # The autotuner picks the 2-D launch shape per grid-size class; the plain
     # path and the server both use its records.
     tuned = {}
-    for n in (256, 512, 1024, 2048, 4096):
-        tuned[n], _ = A.autotune_stencil2d(A.MSL_ST2_JACOBI5, A.MSL_F32, n, n, 1, 100)
-    # plain path: service time of a sample of requests, one at a time
-    rng = np.random.default_rng(5)
-    sample = sorted(rng.choice(len(reqs), size=min(args.serve_plain_sample, len(reqs)), replace=False).tolist())
-    service = []
-    for i in sample:
+    for c in range(12, 25):  # every grid-size class of the 2-D requests (64^2 .. 4096^2 cells)
+        n = int(round(2 ** (c / 2)))
+        d, rows, _ = A.autotune_stencil2d_shape(A.MSL_ST2_JACOBI5, A.MSL_F32, n, n, 1, 100)
+        tuned[n] = f"depth {d}, 64x{rows}"
+
+    def plain_solve(i):
         x = init_of(i)
         kind = A.MSL_ST3_HEAT7 if x.ndim == 3 else A.MSL_ST2_JACOBI5
         a, b = A.DeviceArray.from_host(x), A.DeviceArray(x.shape, np.float32)
-        A.sync()
-        t0 = time.perf_counter()
         out, _, _ = A.solve_plain(kind, a, b, tol, cap, check)
         out.download()
-        service.append(time.perf_counter() - t0)
-    plain_capacity = len(service) / sum(service)
+
+    # plain capacity: service time of a sample of requests, one at a time
+    rng = np.random.default_rng(5)
+    sample = sorted(rng.choice(len(reqs), size=min(args.serve_plain_sample, len(reqs)), replace=False).tolist())
+    t0 = time.perf_counter()
+    for i in sample:
+        plain_solve(i)
+    plain_capacity = len(sample) / (time.perf_counter() - t0)
 
     def plain_queue(arrivals):
-        """FIFO replay of the plain path with service times drawn from the sample."""
-        r = np.random.default_rng(9)
-        t_free, lat = 0.0, []
-        for a in arrivals:
-            start = max(a, t_free)
-            t_free = start + service[int(r.integers(len(service)))]
-            lat.append(t_free - a)
-        return len(arrivals) / (t_free - arrivals[0]), lat
+        """The plain path served for real: FIFO, one request at a time."""
+        t0, lat = time.perf_counter(), []
+        for i, a in enumerate(arrivals):
+            now = time.perf_counter() - t0
+            if a > now:
+                time.sleep(a - now)
+            plain_solve(i)
+            lat.append(time.perf_counter() - t0 - a)
+        return len(arrivals) / (time.perf_counter() - t0), lat
 
     sweep = []
     for factor in args.serve_rates:
@@ -824,6 +837,7 @@ def run_serve(args, dist: Dist):
                       "served_queue_p99_s": float(np.percentile(queued, 99)), "intervals": st["intervals"],
                       "plain_solves_per_s": p_rate, "plain_p50_s": float(np.percentile(p_lat, 50)),
                       "plain_p99_s": float(np.percentile(p_lat, 99))})
+        print(json.dumps(sweep[-1]), file=sys.stderr, flush=True)
     top = sweep[-1]
     if dist.rank == 0:
         line = {"metric": "served stencil solves/s", "value": top["served_solves_per_s"], "unit": "solves/s",
@@ -832,8 +846,9 @@ def run_serve(args, dist: Dist):
                 "config": {"workload": f"{len(reqs)} requests: half 2-D Jacobi n^2 (n log-uniform [64,4096]), half "
                                        f"3-D heat m^3 (m log-uniform [32,256]); U[0,1) init; residual <= {tol} "
                                        f"every {check} sweeps or {cap} sweeps; HBM budget 120 GB; Poisson arrivals",
-                           "plain_capacity_per_s": plain_capacity, "plain_sample": len(service),
-                           "jacobi_temporal_depth_by_side": tuned},
+                           "plain_capacity_per_s": plain_capacity, "plain_capacity_sample": len(sample),
+                           "plain_path": "served for real, FIFO, same arrivals",
+                           "jacobi_launch_shape_by_side": tuned},
                 "sweep": sweep, "served_over_plain_at_top_rate": top["served_solves_per_s"] / top["plain_solves_per_s"]}
         print(json.dumps(line), flush=True)
 
@@ -897,6 +912,7 @@ def run_batch(args, dist: Dist):
             "solved": f"{solved}/{w.count}",
             "e2e": {"value": solved / e2e_s, "unit": w.unit, "h2d_bytes_per_step": w.h2d, "d2h_bytes_per_step": w.d2h},
             "plain_path": {"value": plain_rate, "unit": w.unit, "seconds_all_grids": plain_s,
+                           "seconds_by_side": getattr(w, "plain_by_side", None),
                            "grids": "all, one at a time", "batched_over_plain": value / plain_rate},
             "convergence": summ, "effective_GCUPS": gcups,
             "max_error_vs_fp64": {"grids": f"all {w.count}, FP64 Jacobi of the same sweep count on the GPU",

@@ -44,6 +44,7 @@ namespace {
 using Clock = std::chrono::steady_clock;
 constexpr int kMaxActive = 4096;  // active requests of each kind
 constexpr size_t kResidentSmem = 200 * 1024;  // both iterates of a shared-memory-resident 2-D request
+constexpr int kFewRequests = 4;  // at most this many requests of a kind in an interval: one-request kernels
 
 enum ReqState { kQueued = 0, kRunning = 1, kDone = 2, kFailed = 3, kCancelled = 4 };
 
@@ -191,8 +192,18 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
     };
     std::vector<Request *> big2, big3;
     const long long big_items = 2LL * s.sm_count;  // a request this large fills the GPU on its own
+    // With only a few requests of a kind in the interval, batching them gains
+    // nothing: each runs the one-request kernels, as the plain path would
+    // (the resident kernel, one CTA per grid, would leave the GPU idle).
+    int count2 = 0, count3 = 0;
+    for (Request *r : act) (r->kind == MSL_SERVE_JACOBI2D ? count2 : count3)++;
+    const bool alone2 = count2 <= kFewRequests, alone3 = count3 <= kFewRequests;
     for (Request *r : act) {
         if (r->kind == MSL_SERVE_JACOBI2D) {
+            if (alone2) {
+                big2.push_back(r);
+                continue;
+            }
             const size_t need = 2 * ((r->cells() * sizeof(float) + 127) / 128 * 128);
             if (need <= kResidentSmem) {  // whole grid in shared memory: one launch per interval
                 res2.push_back(r);
@@ -214,7 +225,7 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
         } else {
             const long long nb = (long long)((r->cols + kT3BX - 1) / kT3BX) * ((r->rows + kT3BY - 1) / kT3BY) *
                                  ((r->depth + kT3BZ - 1) / kT3BZ);
-            if (nb >= big_items) {
+            if (alone3 || nb >= big_items) {
                 big3.push_back(r);
                 continue;
             }
