@@ -253,6 +253,16 @@ class StencilSuite:
         # The autotuner picks the temporal depth (sweeps per launch) for the
         # iterated 2-D part; its records are used by the timed iterate calls.
         self.tuned = {}
+        if "heat" in self.parts:
+            # heat3D runs `k` sweeps per launch (msl_set_stencil3d_depth): the
+            # algorithmic bytes of a launch are those of its k sweeps, its
+            # compulsory bytes one read and one write of the cube
+            k = max(1, getattr(self, "heat_sweeps_per_launch", 1))
+            p = self.parts["heat"]
+            p.launches = self.heat_steps // k + self.heat_steps % k
+            p.bytes_per_launch = 8 * m ** 3 * self.heat_steps // p.launches
+            p.sweeps_per_launch = k
+            self.tuned["heat_sweeps_per_launch"] = k
         if "life" in self.parts:
             d = getattr(self, "fixed_depth", 0)
             if d <= 0:
@@ -931,7 +941,8 @@ def life_launches(steps, depth):
 
 
 DRAM_TRAFFIC_PER_LAUNCH = {
-    "heat3d": 1027.49e6,         # profiles/heat7_stencil3d_512.md (one sweep of 512^3)
+    "heat3d": 1059.34e6,         # profiles/heat7_zmarch_512.md (two sweeps of 512^3 per launch)
+    "heat3d/1": 1027.49e6,       # profiles/heat7_stencil3d_512.md (one sweep of 512^3)
     "life": 480.17e6,            # profiles/life_bits_stencil2d_8192.md (32 generations of 8192^2)
     "box_mean_r1-10": 495.08e6,  # profiles/boxmean_r10_box2d_pair_8192.md (r = 10)
 }
@@ -954,8 +965,8 @@ def main():
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[0.25, 0.5, 1.0, 2.0])
     ap.add_argument("--temporal-depth", type=int, default=0,
                     help="sweeps per launch of the iterated 2-D stencils (0: the autotuner's choice)")
-    ap.add_argument("--stencil3d-depth", type=int, default=1, choices=[1, 2],
-                    help="heat3D sweeps per launch: 1 one sweep (default), 2 the z-marching kernel")
+    ap.add_argument("--stencil3d-depth", type=int, default=2, choices=[1, 2],
+                    help="heat3D sweeps per launch: 2 the z-marching kernel (default), 1 one sweep")
     ap.add_argument("--stencil3d-persistent", type=int, default=-1, choices=[-1, 0, 1],
                     help="3-D stencil kernel: 1 persistent, 0 one CTA per block, -1 library default")
     ap.add_argument("--elements", type=int, default=0,
@@ -985,6 +996,7 @@ def main():
     w = MapZipFold(A, args.elements) if args.workload == "mapzipfold" and args.elements > 0 \
         else WORKLOADS[args.workload](A)
     w.fixed_depth = args.temporal_depth  # > 0: no autotuning of the Life depth
+    w.heat_sweeps_per_launch = args.stencil3d_depth
     w.setup()
     if args.temporal_depth > 0:  # after setup: overrides the autotuner's record
         A.set_temporal_depth(args.temporal_depth)
@@ -1058,7 +1070,7 @@ def main():
             parts_out[pp.name]["GCUPS"] = pp.updates / t / 1e9 if t > 0 else None
     # DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum +
     # dram__bytes_write.sum) from the ncu captures summarised in profiles/.
-    traffic = DRAM_TRAFFIC_PER_LAUNCH.get(p.name)
+    traffic = DRAM_TRAFFIC_PER_LAUNCH.get(p.name if getattr(p, "sweeps_per_launch", 2) != 1 else p.name + "/1")
     if p.name == "life" and getattr(w, "tuned", {}).get("life_temporal_depth") != 32:
         traffic = None  # captured at temporal depth 32
 
@@ -1085,7 +1097,8 @@ def main():
                          "bytes_per_launch": p.bytes_per_launch,
                          # several sweeps per launch: the grid's one read and write per launch
                          "compulsory_bytes_per_launch": p.compulsory_bytes,
-                         "compulsory_frac": p.compulsory_bytes / avg_launch_s / 1e9 / peak},
+                         "compulsory_frac": p.compulsory_bytes / avg_launch_s / 1e9 / peak,
+                         **({"sweeps_per_launch": p.sweeps_per_launch} if hasattr(p, "sweeps_per_launch") else {})},
             "parts": parts_out,
             **({"fold_kernel_only": {k: dict(v, frac=v["GB_per_s"] / peak) for k, v in kernel_only.items()}}
                if kernel_only else {}),

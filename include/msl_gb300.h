@@ -265,12 +265,16 @@ int msl_set_tma(int enabled);
  * 0 = one CTA per 64 x 16 x 8 block, -1 = the library's default (one CTA per
  * block). Results are identical either way. */
 int msl_set_stencil3d_persistent(int mode);
-/* Sweeps per launch of msl_stencil3d_iterate for heat3D (FP32, radius 1,
- * neutral 0) on grids TMA can address: 2 = the z-marching kernel, which keeps
- * the first sweep of each pair in shared memory and halves the HBM traffic;
- * 1 (default) = one sweep per launch, faster on GB300 (the z-marching kernel
- * is bound by instruction issue). Results are identical either way. */
+/* Sweeps per launch of msl_stencil3d_iterate (and of the server's large
+ * cubes) for heat3D (FP32, radius 1, neutral 0) on grids TMA can address:
+ * 2 (default) = the z-marching kernel, which keeps the first sweep of each
+ * pair in shared memory and halves the HBM traffic per sweep; 1 = one sweep
+ * per launch. Results are identical either way. */
 int msl_set_stencil3d_depth(int sweeps);
+/* z planes each CTA of the z-marching kernel marches through (0, the
+ * default: chosen per grid so that the CTAs fill whole waves; else 1..1024).
+ * A tuning knob only: results are identical for every value. */
+int msl_set_stencil3d_zchunk(int planes);
 /* Sweeps fused into one launch by msl_stencil2d_iterate (temporal blocking:
  * the CTA runs depth-1 sweeps on a shared-memory tile with a depth*r halo and
  * writes the last; results are identical to single sweeps). 0 (default) uses

@@ -61,7 +61,7 @@ def load() -> ctypes.CDLL:
         "msl_init": [i], "msl_terminate": [], "msl_sync": [], "msl_get_stream": [ctypes.POINTER(vp)],
         "msl_set_stream": [vp], "msl_device_info": [ip, ctypes.POINTER(sz), ctypes.POINTER(sz)],
         "msl_launch_count": [ctypes.POINTER(ctypes.c_ulonglong)], "msl_set_tma": [i],
-        "msl_set_stencil3d_persistent": [i], "msl_set_stencil3d_depth": [i],
+        "msl_set_stencil3d_persistent": [i], "msl_set_stencil3d_depth": [i], "msl_set_stencil3d_zchunk": [i],
         "msl_alloc": [ctypes.POINTER(vp), sz], "msl_free": [vp], "msl_upload": [vp, vp, sz],
         "msl_download": [vp, vp, sz], "msl_copy": [vp, vp, sz], "msl_fill": [i, vp, sz, d],
         "msl_upload_async": [vp, vp, sz, vp], "msl_download_async": [vp, vp, sz, vp],
@@ -148,8 +148,13 @@ def set_stencil3d_persistent(mode: int) -> None:
 
 
 def set_stencil3d_depth(sweeps: int) -> None:
-    """heat3D sweeps per launch: 1 one sweep (default), 2 the z-marching kernel."""
+    """heat3D sweeps per launch: 2 the z-marching kernel (default), 1 one sweep."""
     check(load().msl_set_stencil3d_depth(int(sweeps)), "msl_set_stencil3d_depth")
+
+
+def set_stencil3d_zchunk(planes: int) -> None:
+    """z planes per CTA of the z-marching heat3D kernel (0 = chosen per grid)."""
+    check(load().msl_set_stencil3d_zchunk(int(planes)), "msl_set_stencil3d_zchunk")
 
 
 def set_temporal_depth(depth: int) -> None:

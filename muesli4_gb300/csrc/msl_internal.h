@@ -59,6 +59,12 @@ int tuned_depth(int dtype, int kind, int rows, int cols, int radius);
 // when none is recorded.
 int tuned_tile_rows(int dtype, int kind, int rows, int cols, int radius);
 
+// heat3D sweeps per launch (msl_set_stencil3d_depth, stencil.cu): nonzero when
+// pairs of sweeps run on the z-marching kernel; its z planes per CTA (0: chosen
+// per grid).
+int stencil3d_pair_sweeps();
+int stencil3d_zchunk();
+
 }  // namespace rt
 }  // namespace msl
 

@@ -57,6 +57,7 @@ struct Request {
     size_t bytes = 0;  // both iterates
     void *buf[2] = {nullptr, nullptr};
     int cur = 0;
+    int launches = 0;  // launches of the last interval on the one-request kernels (buffer flips)
     long long iters = 0;
     double residual = 0.0;
     int waited = 0;          // consecutive intervals this running request was not scheduled
@@ -296,6 +297,7 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
             const int depth = rt::tuned_depth(MSL_F32, MSL_ST2_JACOBI5, r->rows, r->cols, 1);
             const int tile_rows = rt::tuned_tile_rows(MSL_F32, MSL_ST2_JACOBI5, r->rows, r->cols, 1);
             float *p = (float *)r->buf[r->cur], *q = (float *)r->buf[r->cur ^ 1];
+            r->launches = 0;
             for (int i = 0; i < s.check_every;) {
                 const int d = std::min(std::max(depth, 1), s.check_every - i);
                 unsigned long long *resid = i + d == s.check_every ? &dg->resid_bits : nullptr;
@@ -330,16 +332,36 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
             SERVE_TRY(cudaGetLastError());
             rt::count_launch(s.check_every);
         }
+        const bool pairs = rt::stencil3d_pair_sweeps() != 0;
         for (size_t k = 0; k < big3.size(); k++) {  // as msl_stencil3d_iterate runs a cube alone
             Request *r = big3[k];
             ServeCube *dc = s.d3 + n3b + (int)k;
             float *p = (float *)r->buf[r->cur], *q = (float *)r->buf[r->cur ^ 1];
-            for (int i = 0; i < s.check_every; i++) {
-                unsigned long long *resid = i + 1 == s.check_every ? &dc->resid_bits : nullptr;
-                SERVE_TRY(launch_stencil3d<float>(p, q, r->depth, r->rows, r->cols, 1, 0.0f, Heat7Fn{}, resid, s.d_err,
-                                                  s.s3, s.sm_count));
-                rt::count_launch();
+            r->launches = 0;
+            for (int i = 0; i < s.check_every;) {
+                // two sweeps per launch on the z-marching kernel where it applies
+                const int n = pairs && i + 2 <= s.check_every ? 2 : 1;
+                unsigned long long *resid = i + n == s.check_every ? &dc->resid_bits : nullptr;
+                cudaError_t e = cudaErrorNotSupported;
+                if (n == 2)
+                    e = launch_stencil3d_ztb(p, q, r->depth, r->rows, r->cols, Heat7Fn{}, resid, s.d_err, s.s3,
+                                             rt::stencil3d_zchunk());
+                if (e == cudaErrorNotSupported) {  // one sweep (a grid TMA cannot address: each sweep alone)
+                    for (int j = 0; j < n; j++) {
+                        unsigned long long *rj = j + 1 == n ? resid : nullptr;
+                        SERVE_TRY(launch_stencil3d<float>(p, q, r->depth, r->rows, r->cols, 1, 0.0f, Heat7Fn{}, rj,
+                                                          s.d_err, s.s3, s.sm_count));
+                        rt::count_launch();
+                        r->launches++;
+                        if (j + 1 < n) std::swap(p, q);
+                    }
+                } else {
+                    SERVE_TRY(e);
+                    rt::count_launch();
+                    r->launches++;
+                }
                 std::swap(p, q);
+                i += n;
             }
         }
         SERVE_TRY(cudaMemcpyAsync(s.h3.data(), s.d3, n3 * sizeof(ServeCube), cudaMemcpyDeviceToHost, s.s3));
@@ -372,7 +394,7 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
     for (int i = 0; i < n3; i++) {
         Request *r = r3[i];
         if (i >= n3b) {
-            advance(r, s.h3[i].resid_bits, s.check_every);
+            advance(r, s.h3[i].resid_bits, r->launches);
             continue;
         }
         r->cur = s.h3[i].cur;

@@ -27,10 +27,12 @@ struct Sweep {
 // 3-D kernel choice of msl_set_stencil3d_persistent (-1 = default).
 std::atomic<int> g_persistent3d{-1};
 // Sweeps per launch of msl_stencil3d_iterate where the z-marching kernel
-// applies (1 or 2). One sweep per launch is the default: on heat3D 512^3 the
-// one-sweep kernel runs at the HBM roofline (786 GCUPS) while the z-marching
-// kernel, with half the HBM traffic, is bound by instruction issue (660).
-std::atomic<int> g_depth3d{1};
+// applies (1 or 2). Two is the default: on heat3D 512^3 the two-sweep kernel
+// (half the HBM traffic per sweep, bound by instruction issue) runs 1.4x the
+// one-sweep kernel, which is itself at the HBM roofline.
+std::atomic<int> g_depth3d{2};
+// z planes per CTA of the z-marching kernel (0: chosen per grid).
+std::atomic<int> g_zchunk3d{0};
 
 template <typename S>
 cudaError_t sweep2d(int kind, const S *in, S *out, int rows, int cols, int r, double neutral_d, const Sweep &sw) {
@@ -200,6 +202,13 @@ int depth_for(int dtype, int kind, int rows, int cols, int r) {
 
 }  // namespace
 
+namespace msl {
+namespace rt {
+int stencil3d_pair_sweeps() { return g_depth3d.load(std::memory_order_relaxed) == 2; }
+int stencil3d_zchunk() { return g_zchunk3d.load(std::memory_order_relaxed); }
+}  // namespace rt
+}  // namespace msl
+
 extern "C" {
 
 int msl_set_tma(int enabled) {
@@ -210,6 +219,13 @@ int msl_set_tma(int enabled) {
 int msl_set_stencil3d_depth(int sweeps) {
     if (sweeps < 1 || sweeps > 2) return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_set_stencil3d_depth: %d not 1 or 2", sweeps);
     g_depth3d.store(sweeps);
+    return MSL_OK;
+}
+
+int msl_set_stencil3d_zchunk(int planes) {
+    if (planes < 0 || planes > 1024)
+        return rt::fail(MSL_ERR_INVALID_ARGUMENT, "msl_set_stencil3d_zchunk: %d not in 0..1024", planes);
+    g_zchunk3d.store(planes);
     return MSL_OK;
 }
 
@@ -305,7 +321,8 @@ int msl_stencil3d_iterate(int dtype, int kind, void *a, void *b, int depth, int 
                    [&](void *p, void *q, int k, const Sweep &sw) {
                        if (k == 2)
                            return launch_stencil3d_ztb((const float *)p, (float *)q, depth, rows, cols,
-                                                       StHeat7<float>{}, sw.resid, ctx().err_word, ctx().stream);
+                                                       StHeat7<float>{}, sw.resid, ctx().err_word, ctx().stream,
+                                                       g_zchunk3d.load(std::memory_order_relaxed));
                        return dispatch3d(dtype, kind, p, q, depth, rows, cols, radius, neutral, sw);
                    });
 }

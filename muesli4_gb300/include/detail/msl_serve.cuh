@@ -9,6 +9,7 @@
 #pragma once
 
 #include "msl_batch.cuh"
+#include "msl_stencil3d_tb.cuh"
 
 namespace msl {
 namespace gpu {
@@ -26,15 +27,18 @@ struct ServeCube {
 // heat3D (examples/heatdiffusion.cpp:55-65), Dirichlet 0 outside the cube.
 struct Heat7Fn {
     static constexpr bool kStar7 = true;
-    __device__ __forceinline__ float star7(float w, float e, float n, float s, float b, float f) const {
+    static constexpr bool kSum7Div6 = true;
+    __device__ __forceinline__ float sum7(float w, float e, float n, float s, float b, float f) const {
         float v = 0.0f;
         v = __fadd_rn(v, w);
         v = __fadd_rn(v, e);
         v = __fadd_rn(v, n);
         v = __fadd_rn(v, s);
         v = __fadd_rn(v, b);
-        v = __fadd_rn(v, f);
-        return div6_rn(v);
+        return __fadd_rn(v, f);
+    }
+    __device__ __forceinline__ float star7(float w, float e, float n, float s, float b, float f) const {
+        return div6_rn(sum7(w, e, n, s, b, f));
     }
     template <class V> __device__ __forceinline__ float operator()(const V &c, int x, int y, int z) const {
         return star7(c(x - 1, y, z), c(x + 1, y, z), c(x, y - 1, z), c(x, y + 1, z), c(x, y, z - 1), c(x, y, z + 1));

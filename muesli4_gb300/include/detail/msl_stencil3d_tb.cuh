@@ -1,27 +1,41 @@
 // Two sweeps per launch of a 7-point 3-D stencil (heat3D) by z-marching:
 // temporal blocking without the z halo of a block.
 //
-// One CTA owns a 64 x 16 column of cells and marches through a chunk of z
-// planes. Each step stages an input plane (window 72 x 20: the column plus
-// two cells on every side in x and y) with one TMA load into a ring of six
-// planes (loads run two steps ahead), computes the first sweep
-// ("intermediate") on the column plus a one-cell margin (66 x 18 cells) into
-// a ring of three planes, and the second sweep on the column from the
-// intermediate planes, straight to HBM. The z
-// halo costs two intermediate planes per chunk instead of two per block;
-// the x/y margin costs 16 % more first-sweep cells. Every thread owns four
-// vertically adjacent cells of the column and keeps their input and
-// intermediate values for three consecutive planes in registers (centre, B
-// and F of both sweeps); W, E, N and S come from shared memory. One barrier
-// per plane.
+// One CTA owns a 64 x 32 (x, y) tile and marches through a chunk of z planes.
+// Step t of the march
+//   * computes the first sweep ("intermediate") at plane t+1 on the tile plus
+//     a one-cell margin into one of two intermediate planes in shared memory:
+//     the tile's cells by register strips, the 192 margin cells (the row above
+//     and below, the column left and right; a star reads no diagonal, so the
+//     corners are not needed) as six whole-warp items;
+//   * computes the second sweep at plane t from the intermediate planes t-1,
+//     t and t+1, straight to HBM;
+// and one barrier ends the step. Input planes (a 72 x 36 window: the tile
+// plus two cells on every side, x rounded out to 16 bytes) arrive by TMA in a
+// ring of four slots, issued two steps before their first use.
+//
+// Every thread owns one column of eight vertically adjacent cells and keeps
+// its input and intermediate values of the three planes a star reads in
+// registers (B, centre and F of both sweeps; N and S inside the strip); W, E
+// and the strip's two ends come from shared memory. The margin lanes keep
+// their input values in registers the same way, so no step reads an input
+// plane older than t+1 and the slot of plane t takes the load of plane t+4 as
+// the step begins. The roles of the register columns rotate with the plane:
+// the march is unrolled three times, so no value is copied between steps.
+//
+// heat3D divides the sum of six neighbours by 6. The sums and the division's
+// fast path (div6_core) run on packed FP32 pairs, two cells per instruction;
+// a warp vote finds the rare sums outside the fast path's range, and only
+// then does the strip divide cell by cell with IEEE division where needed,
+// exactly as star7 would compute it.
 //
 // Requirements (checked by the launcher): FP32 cells, a functor with
-// kStar7 (the six face neighbours; heat3D), neutral value +0 -- outside the
-// grid both the staged input (TMA zero fill) and the intermediate sweep (set
-// explicitly) hold 0, which is exactly the view's neutral value -- and a grid
-// TMA can address. Results are bit-identical to two launches of the one-sweep
-// kernel: every cell of every sweep is computed by the same functor from the
-// same operands; only where the operands live differs.
+// kSum7Div6 (heat3D), neutral value +0 -- outside the grid both the staged
+// input (TMA zero fill) and the intermediate sweep (set explicitly) hold 0,
+// which is exactly the view's neutral value -- and a grid TMA can address.
+// Results are bit-identical to two launches of the one-sweep kernel: every
+// cell of every sweep is computed by the same functor from the same operands;
+// only where the operands live differs.
 #pragma once
 
 #include "msl_stencil.cuh"
@@ -29,259 +43,331 @@
 namespace msl {
 namespace gpu {
 
-constexpr int kZtbChunk = 32;                    // z planes per CTA
-constexpr int kZtbPitch = kT3BX + 8;              // 72: x window (2-cell halo rounded up to 16 bytes)
-constexpr int kZtbRows = kT3BY + 4;               // 20: y window
-constexpr int kZtbPlane = kZtbPitch * kZtbRows;   // floats per staged plane
-constexpr int kZtbIn = 6, kZtbMid = 3;            // ring planes: input (two planes of look-ahead), intermediate
+constexpr int kZtbBX = 64, kZtbBY = 32, kZtbRPT = 8, kZtbThreads = 256;
+constexpr int kZtbPitch = kZtbBX + 8;                    // 72: window x0-4 .. x0+67
+constexpr int kZtbRows = kZtbBY + 4;                     // 36: window y0-2 .. y0+33
+constexpr int kZtbPlane = kZtbPitch * kZtbRows;          // floats per input slot (10368 bytes = 81 x 128)
+constexpr int kZtbMidPlane = kZtbPitch * (kZtbBY + 2);   // intermediate slot: window rows 1 .. 34
+constexpr int kZtbInSlots = 4, kZtbMidSlots = 2;         // plane p in input slot p & 3, intermediate slot p & 1
+constexpr int kZtbMarginWarps = 6;                       // 192 margin cells = six warp items
 
 inline size_t stencil3d_ztb_smem() {
-    return (size_t)kStHeader + (size_t)(kZtbIn + kZtbMid) * kZtbPlane * sizeof(float);
+    return (size_t)kStHeader + ((size_t)kZtbInSlots * kZtbPlane + (size_t)kZtbMidSlots * kZtbMidPlane) * sizeof(float);
 }
 
+// Functors declaring kSum7Div6 compute star7 as sum7 / 6 correctly rounded,
+// with sum7 = (((((0 + w) + e) + n) + s) + b) + f (heat3D).
 template <class Fn, class = void> struct IsSum7Div6 : std::false_type {};
 template <class Fn> struct IsSum7Div6<Fn, std::void_t<decltype(Fn::kSum7Div6)>> : std::bool_constant<Fn::kSum7Div6> {};
 
-// One cell of a sweep. A functor whose value is sum7 / 6 (heat3D) takes the
-// division's fast path here; `ok` is cleared when a live cell's sum lies
-// outside that path's range, and ztb_fixup redoes those cells.
-template <class Fn>
-MSL_DEV float ztb_cell(const Fn &fn, float w, float e, float n, float s, float b, float f, bool live, float &sum,
-                       bool &ok) {
-    if constexpr (IsSum7Div6<Fn>::value) {
-        sum = fn.sum7(w, e, n, s, b, f);
-        ok = ok && (!live || div6_in_range(sum));
-        return div6_core(sum);
-    } else {
-        return fn.star7(w, e, n, s, b, f);
-    }
+// Packed FP32 pairs (add/mul/fma.rn.f32x2: two independent IEEE operations
+// per instruction, each rounded as the scalar one). A thread's strip keeps
+// cells j and j+4 in one pair, so the N and S operands of a pair are again
+// pairs of the strip (all but the strip's two ends).
+using f32x2 = unsigned long long;
+MSL_DEV f32x2 pk2(float a, float b) {
+    f32x2 d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(a), "f"(b));
+    return d;
 }
+MSL_DEV float lo2(f32x2 v) {
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return a;
+}
+MSL_DEV float hi2(f32x2 v) {
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return b;
+}
+MSL_DEV f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+MSL_DEV f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+MSL_DEV f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+// heat3D's sum of six neighbours in its order, (((((0 + w) + e) + n) + s) + b) + f, for a pair.
+MSL_DEV f32x2 sum7x2(f32x2 w, f32x2 e, f32x2 n, f32x2 s, f32x2 b, f32x2 f) {
+    f32x2 v = add2(pk2(0.0f, 0.0f), w);
+    v = add2(v, e);
+    v = add2(v, n);
+    v = add2(v, s);
+    v = add2(v, b);
+    return add2(v, f);
+}
+// div6_core on both halves: q = x * RN(1/6), r = x - 6q (exact), q + r * RN(1/6).
+MSL_DEV f32x2 div6_core2(f32x2 x) {
+    const float zh = 0.16666667163372039794921875f;
+    const f32x2 z2 = pk2(zh, zh);
+    const f32x2 q = mul2(x, z2);
+    const f32x2 r = fma2(q, pk2(-6.0f, -6.0f), x);
+    return fma2(r, z2, q);
+}
+// IEEE-correct x / 6 for sums outside the fast path's range; out of line so
+// that the rare path does not crowd the march's instruction cache.
+static __device__ __noinline__ float div6_cold(float x) { return div6_rn(x); }
 
-// One vote per warp and sweep: if any lane holds a sum outside the fast
-// division's range, those cells take IEEE division.
-template <class Fn, int N>
-MSL_DEV void ztb_fixup(const Fn &, bool ok, const bool (&live)[N], const float (&sum)[N], float (&v)[N]) {
-    if constexpr (IsSum7Div6<Fn>::value) {
-        if (__all_sync(0xFFFFFFFFu, ok)) return;
+// x / 6 for the four pairs of a strip: the fast path for the whole warp when
+// every lane's `good` holds (its live cells' sums lie in the fast path's
+// range), else div6_rn cell by cell (IEEE division outside the range).
+MSL_DEV void div6_pairs(bool good, f32x2 (&x)[4]) {
+    if (__all_sync(0xFFFFFFFFu, good)) {
 #pragma unroll
-        for (int j = 0; j < N; j++)
-            if (live[j] && !div6_in_range(sum[j])) v[j] = __fdiv_rn(sum[j], 6.0f);
+        for (int k = 0; k < 4; k++) x[k] = div6_core2(x[k]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) x[k] = pk2(div6_cold(lo2(x[k])), div6_cold(hi2(x[k])));
     }
 }
 
+#ifndef MSL_ZTB_MIN_CTAS
+#define MSL_ZTB_MIN_CTAS 3
+#endif
 template <class Fn>
-__global__ void __launch_bounds__(kT3Threads, 4)
-    stencil3d_ztb_kernel(const __grid_constant__ CUtensorMap tmap, float *out, int depth, int rows, int cols, Fn fn,
-                         unsigned long long *resid, unsigned *err) {
+__global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
+    stencil3d_ztb_kernel(const __grid_constant__ CUtensorMap tmap, float *out, int depth, int rows, int cols,
+                         int zchunk, Fn fn, unsigned long long *resid, unsigned *err) {
+    static_assert(IsSum7Div6<Fn>::value, "the two-sweep kernel takes sum7 / 6 functors");
+    static_assert(kZtbRPT == 8, "cells j and j+4 of the strip form a pair");
+    constexpr int P = kZtbPitch;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);  // one mbarrier per input slot
     float *in_ring = reinterpret_cast<float *>(smem_raw + kStHeader);
-    float *mid_ring = in_ring + kZtbIn * kZtbPlane;
-    const int x0 = blockIdx.x * kT3BX, y0 = blockIdx.y * kT3BY, zb = blockIdx.z * kZtbChunk;
-    const int ze = min(zb + kZtbChunk, depth);
-    const int wx0 = x0 - 4, wy0 = y0 - 2;  // window origin (x halo 4 for 16-byte TMA alignment)
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // this thread's four cells: window column cx, rows cy .. cy+3
-    const int cx = 4 + (warp & 1) * 32 + lane, cy = 2 + (warp >> 1) * kT3RPT;
-    const int gx = wx0 + cx, gy0 = wy0 + cy;
-    const bool x_in = gx < cols;
-    const bool xy_in = x0 + kT3BX <= cols && y0 + kT3BY <= rows;  // every thread's own cells lie in the grid
-    // margin cell of the first sweep (threads 0 .. 163): window columns 3 and
-    // 68 for rows 1..18, and rows 1 and 18 for columns 4..67
-    int mx = -1, my = -1;
-    {
-        const int t = threadIdx.x;
-        if (t < 36) {
-            mx = t < 18 ? 3 : 4 + kT3BX;
-            my = 1 + (t < 18 ? t : t - 18);
-        } else if (t < 36 + 2 * kT3BX) {
-            const int u = t - 36;
-            mx = 4 + (u % kT3BX);
-            my = u < kT3BX ? 1 : 2 + kT3BY;
-        }
-    }
-    const bool has_margin = mx >= 0;
-    const int mgx = wx0 + mx, mgy = wy0 + my;
-    const bool m_in = has_margin && mgx >= 0 && mgx < cols && mgy >= 0 && mgy < rows;
+    float *mid_ring = in_ring + kZtbInSlots * kZtbPlane;
 
-    // ring slots: input plane p in slot (p + 2) % kZtbIn, intermediate plane
-    // p in slot (p + 1) % kZtbMid; slot indices are advanced step by step
-    auto in_at = [&](int k) { return in_ring + k * kZtbPlane; };
-    auto mid_at = [&](int k) { return mid_ring + k * kZtbPlane; };
-    auto next_in = [](int k) { return k == kZtbIn - 1 ? 0 : k + 1; };
-    auto next_mid = [](int k) { return k == kZtbMid - 1 ? 0 : k + 1; };
-    auto in_slot = [&](int p) { return (p - zb + 2) % kZtbIn; };  // p >= zb - 2; used outside the loop
-    uint32_t pending = 0;  // thread 0: bit k = a load into slot k not yet waited for
-    auto issue = [&](int p) {  // thread 0: TMA load of input plane p (zeros outside the grid)
-        const int k = in_slot(p);
+    // chunk-major order: the CTAs resident together march neighbouring tiles
+    // at the same depth, so the halo lines one fetches are in L2 for the next
+    const unsigned tiles_x = (unsigned)(cols + kZtbBX - 1) / kZtbBX;
+    const unsigned tiles = tiles_x * ((unsigned)(rows + kZtbBY - 1) / kZtbBY);
+    const unsigned tile = blockIdx.x % tiles, chunk = blockIdx.x / tiles;
+    const int x0 = (int)(tile % tiles_x) * kZtbBX, y0 = (int)(tile / tiles_x) * kZtbBY;
+    const int zb = (int)chunk * zchunk, ze = min(zb + zchunk, depth);
+    const int wx0 = x0 - 4, wy0 = y0 - 2;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // the thread that issues and waits for the TMA loads: lane 0 of the last
+    // warp, which has no margin item
+    const bool leader = threadIdx.x == kZtbThreads - 32;
+
+    // this thread's strip: window column cx, rows cy .. cy+7
+    const int cx = 4 + (warp & 1) * 32 + lane, cy = 2 + (warp >> 1) * kZtbRPT;
+    const int gx = wx0 + cx, gy0 = wy0 + cy;
+    const int own = cy * P + cx, own_mid = own - P;  // intermediate slots start at window row 1
+    const bool x_in = gx < cols;
+    // every strip cell lies inside the grid (margin cells are tested one by one)
+    const bool full = x0 + kZtbBX <= cols && y0 + kZtbBY <= rows;
+
+    // margin item of warps 0..5: rows 1 and 34 over columns 4..67 (warps
+    // 0-3), columns 3 and 68 over rows 2..33 (warps 4-5, half a warp each)
+    const bool has_margin = warp < kZtbMarginWarps;
+    int mx = cx, my = cy;
+    if (warp < 4) {
+        mx = 4 + (warp & 1) * 32 + lane;
+        my = warp < 2 ? 1 : kZtbBY + 2;
+    } else if (has_margin) {
+        mx = lane < 16 ? 3 : kZtbBX + 4;
+        my = 2 + (warp - 4) * 16 + (lane & 15);
+    }
+    const int mo = my * P + mx, mo_mid = mo - P;
+    const bool m_in = wx0 + mx >= 0 && wx0 + mx < cols && wy0 + my >= 0 && wy0 + my < rows;
+
+    uint32_t phase = 0, pending = 0;  // leader: per slot, the parity of its next completion / a load not waited for
+    auto slot = [&](int p) { return in_ring + (p & 3) * kZtbPlane; };
+    auto issue = [&](int p) {  // leader: TMA load of input plane p (zeros outside the grid)
+        const int k = p & 3;
         pending |= 1u << k;
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&bar[k], (uint32_t)(kZtbPlane * sizeof(float)));
-        tma_load_3d(in_at(k), &tmap, &bar[k], wx0, wy0, p);
+        tma_load_3d(slot(p), &tmap, &bar[k], wx0, wy0, p);
     };
-    // Only thread 0 waits for a plane (the other warps sleep at the barrier
-    // that follows instead of polling); the barrier then makes the plane
-    // visible to every thread.
-    uint32_t phase = 0;  // thread 0: bit k = parity of the next completion of slot k
-    auto wait_slot = [&](int k) {
-        if (threadIdx.x != 0) return true;
+    // Only the leader waits for a plane (the other warps sleep at the barrier
+    // that follows instead of polling); the barrier makes it visible to all.
+    auto wait_plane = [&](int p) {
+        const int k = p & 3;
         const bool ok = mbar_wait_bounded(&bar[k], (phase >> k) & 1u, err);  // the load has landed either way
         phase ^= 1u << k;
         pending &= ~(1u << k);
         return ok;
     };
+    auto drain = [&]() {  // leader, on failure: loads in flight land before the CTA gives up its shared memory
+        for (int k = 0; k < kZtbInSlots; k++)
+            if (pending & (1u << k)) mbar_poll(&bar[k], (phase >> k) & 1u, kMaxWaitPolls);
+    };
 
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < kZtbIn; k++) mbar_init(&bar[k], 1);
+    if (leader) {
+        for (int k = 0; k < kZtbInSlots; k++) mbar_init(&bar[k], 1);
         fence_barrier_init();
     }
     __syncthreads();
-    // prologue loads: input planes zb-2 .. zb+kZtbIn-3 (each plane zb-2 .. ze+1
-    // is loaded once and waited for once)
-    if (threadIdx.x == 0)
-        for (int p = zb - 2; p <= min(zb + kZtbIn - 3, ze + 1); p++) issue(p);
-
-    using Col = float[kT3RPT];
-    auto load_col = [&](Col &dst, const float *plane) {
-        const float *q = plane + cy * kZtbPitch + cx;
-#pragma unroll
-        for (int j = 0; j < kT3RPT; j++) dst[j] = q[j * kZtbPitch];
-    };
-    // First sweep at plane p for this thread's cells and margin cell from
-    // input planes pb = p-1, pc = p, pf = p+1 (staged; the own column's values
-    // in registers cb, cc, cf). Writes the intermediate plane (0 outside the
-    // grid) to `m` and this thread's values to `res`. FULL: plane p and the
-    // thread's own cells lie inside the grid (no per-cell tests).
-    auto first_sweep = [&](auto full_tag, int p, const float *pb, const float *pc, const float *pf, const Col &cb,
-                           const Col &cc, const Col &cf, float *m, Col &res) {
-        constexpr bool FULL = decltype(full_tag)::value;
-        const bool p_in = FULL || (p >= 0 && p < depth);
-        const float *q = pc + cy * kZtbPitch + cx;
-        const float n = q[-kZtbPitch], s = q[kT3RPT * kZtbPitch];
-        float sum[kT3RPT + 1], v[kT3RPT + 1];
-        bool live[kT3RPT + 1];
-        bool ok = true;
-#pragma unroll
-        for (int j = 0; j < kT3RPT; j++) {
-            live[j] = FULL || (p_in && x_in && gy0 + j < rows);
-            v[j] = ztb_cell(fn, q[j * kZtbPitch - 1], q[j * kZtbPitch + 1], j == 0 ? n : cc[j - 1],
-                            j == kT3RPT - 1 ? s : cc[j + 1], cb[j], cf[j], live[j], sum[j], ok);
-        }
-        const int o = has_margin ? my * kZtbPitch + mx : 0;
-        live[kT3RPT] = has_margin && p_in && m_in;
-        v[kT3RPT] = 0.0f;
-        sum[kT3RPT] = 0.0f;
-        if (has_margin)
-            v[kT3RPT] = ztb_cell(fn, pc[o - 1], pc[o + 1], pc[o - kZtbPitch], pc[o + kZtbPitch], pb[o], pf[o],
-                                 live[kT3RPT], sum[kT3RPT], ok);
-        ztb_fixup(fn, ok, live, sum, v);
-#pragma unroll
-        for (int j = 0; j < kT3RPT; j++) {
-            const float x = live[j] ? v[j] : 0.0f;
-            res[j] = x;
-            m[(cy + j) * kZtbPitch + cx] = x;
-        }
-        if (has_margin) m[o] = live[kT3RPT] ? v[kT3RPT] : 0.0f;
-    };
-
-    // Registers: three input columns and three intermediate columns whose
-    // roles rotate with the plane (the loop below is unrolled three times so
-    // that every role is a fixed register array: no copies between steps).
-    Col ca, cb, cc;  // input columns
-    Col ma, mb, mc;  // intermediate columns
+    // Input planes zb-2 .. ze+1 are each loaded once and waited for once:
+    // the first four here, plane t+4 at step t, waited for at step t+1.
     bool ok = true;
-    int kin = 0, kmid = 0;  // slot of input plane t-1 and of intermediate plane t-1 at step t
-    // prologue: intermediate planes zb-1 and zb, from input planes zb-2 .. zb+1
-    {
-        const int k0 = 0, k1 = 1, k2 = 2, k3 = 3;  // slots of input planes zb-2 .. zb+1
-        ok = wait_slot(k0) && wait_slot(k1) && wait_slot(k2);
-        ok = __syncthreads_and(ok);
-        if (ok) {
-            load_col(ca, in_at(k0));
-            load_col(cb, in_at(k1));
-            load_col(cc, in_at(k2));
-            first_sweep(std::false_type{}, zb - 1, in_at(k0), in_at(k1), in_at(k2), ca, cb, cc, mid_at(0), mb);
-            ok = wait_slot(k3);
-        }
-        ok = __syncthreads_and(ok);
-        if (ok) {
-            load_col(ca, in_at(k3));  // plane zb+1 takes the place of zb-2
-            first_sweep(std::false_type{}, zb, in_at(k1), in_at(k2), in_at(k3), cb, cc, ca, mid_at(1), mc);
-            ok = wait_slot(4);  // input plane zb+2, read by step zb
-        }
-        ok = __syncthreads_and(ok);  // intermediate planes zb-1 and zb visible
-        kin = k1;                    // input plane zb-1
-        kmid = 0;                    // intermediate plane zb-1
+    if (leader) {
+        for (int p = zb - 2; p <= zb + 1; p++) issue(p);
+        ok = wait_plane(zb - 2);
+        ok = wait_plane(zb - 1) && ok;
+        ok = wait_plane(zb) && ok;
     }
-    // now: cb = input zb-1, cc = input zb, ca = input zb+1; mb = intermediate
-    // zb-1, mc = intermediate zb; ma is free
+    if (!__syncthreads_and(ok)) {
+        if (leader) drain();
+        return;
+    }
 
-    double dmax = 0.0;
+    // register columns, pair k = cells k and k+4 of the strip
+    auto load_col = [&](f32x2 (&d)[4], const float *plane) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) d[k] = pk2(plane[own + k * P], plane[own + (k + 4) * P]);
+    };
+    f32x2 ia[4], ib[4], ic[4];  // input columns
+    f32x2 ma[4], mb[4], mc[4];  // intermediate columns
+    float pa = 0.0f, pb = 0.0f, pc = 0.0f;  // the margin cell's input values
+    load_col(ia, slot(zb - 2));
+    load_col(ib, slot(zb - 1));
+    if (has_margin) {
+        pa = slot(zb - 2)[mo];
+        pb = slot(zb - 1)[mo];
+    }
+    __syncthreads();  // plane zb-2's slot is read before step zb-2 reloads it
+
     const bool want = resid != nullptr;
-    // Step t (final plane t; input plane t+2 is staged and visible). Input
-    // roles: xb = plane t, xc = t+1, xf gets t+2; intermediate roles: yb =
-    // t-1, yc = t, yf gets t+1.
-    auto step = [&](int t, Col &xb, Col &xc, Col &xf, Col &yb, Col &yc, Col &yf) {
-        const int s0 = next_in(kin), s1 = next_in(s0), s2 = next_in(s1);  // input planes t, t+1, t+2
-        const int m1 = next_mid(kmid), m2 = next_mid(m1);                 // intermediate planes t, t+1
-        // the slot of plane t-2 is free since step t-2: load plane t+4 into it
-        if (threadIdx.x == 0 && t + kZtbIn - 2 <= ze + 1) issue(t + kZtbIn - 2);
-        load_col(xf, in_at(s2));
-        if (xy_in && t + 1 < depth)
-            first_sweep(std::true_type{}, t + 1, in_at(s0), in_at(s1), in_at(s2), xb, xc, xf, mid_at(m2), yf);
-        else
-            first_sweep(std::false_type{}, t + 1, in_at(s0), in_at(s1), in_at(s2), xb, xc, xf, mid_at(m2), yf);
-        // second sweep at plane t from intermediate planes t-1, t, t+1
-        const float *q = mid_at(m1) + cy * kZtbPitch + cx;
-        const float n = q[-kZtbPitch], s = q[kT3RPT * kZtbPitch];
-        float sum[kT3RPT], v[kT3RPT];
-        bool live[kT3RPT];
-        bool ok2 = true;
+    double dmax = 0.0;
+    auto live_row = [&](auto full_tag, int j) {
+        constexpr bool FULL = decltype(full_tag)::value;
+        return FULL || (x_in && gy0 + j < rows);
+    };
+    // One sweep of the strip: W, E and the strip's ends from the plane in
+    // shared memory (q: the strip's first cell, rows P apart), B, the centre
+    // (N and S inside the strip) and F from the register columns cb, cc, cf:
+    // the four pairs' sums, then x / 6.
+    auto sweep = [&](auto full_tag, const float *q, const f32x2 (&cb)[4], const f32x2 (&cc)[4],
+                     const f32x2 (&cf)[4], f32x2 (&v)[4]) {
+        const float n = q[-P], s = q[kZtbRPT * P];
+        bool good = true;
 #pragma unroll
-        for (int j = 0; j < kT3RPT; j++) {
-            live[j] = xy_in || (x_in && gy0 + j < rows);
-            v[j] = ztb_cell(fn, q[j * kZtbPitch - 1], q[j * kZtbPitch + 1], j == 0 ? n : yc[j - 1],
-                            j == kT3RPT - 1 ? s : yc[j + 1], yb[j], yf[j], live[j], sum[j], ok2);
+        for (int k = 0; k < 4; k++) {
+            const f32x2 w = pk2(q[k * P - 1], q[(k + 4) * P - 1]);
+            const f32x2 e = pk2(q[k * P + 1], q[(k + 4) * P + 1]);
+            const f32x2 nn = k == 0 ? pk2(n, lo2(cc[3])) : cc[k - 1];
+            const f32x2 ss = k == 3 ? pk2(hi2(cc[0]), s) : cc[k + 1];
+            v[k] = sum7x2(w, e, nn, ss, cb[k], cf[k]);
+            good = good && (!live_row(full_tag, k) || div6_in_range(lo2(v[k])));
+            good = good && (!live_row(full_tag, k + 4) || div6_in_range(hi2(v[k])));
         }
-        ztb_fixup(fn, ok2, live, sum, v);
-        float *o = out + ((size_t)t * rows + gy0) * cols + gx;
+        div6_pairs(good, v);
+    };
+    // Step t: intermediate plane t+1 (from input planes t, t+1, t+2), then
+    // output plane t (from intermediate planes t-1, t, t+1) when t >= zb.
+    // Input roles: xb = plane t, xc = t+1, xf <- t+2; intermediate roles:
+    // yb = t-1, yc = t, yf <- t+1; margin: qb = plane t, qf <- t+2.
+    auto step = [&](auto full_tag, auto want_tag, int t, f32x2 (&xb)[4], f32x2 (&xc)[4], f32x2 (&xf)[4],
+                    f32x2 (&yb)[4], f32x2 (&yc)[4], f32x2 (&yf)[4], float &qb, float &qf) {
+        constexpr bool FULL = decltype(full_tag)::value, WANT = decltype(want_tag)::value;
+        if (leader && t + 4 <= ze + 1) issue(t + 4);  // into the slot of plane t, last read at step t-1
+        const float *pc_ = slot(t + 1), *pf_ = slot(t + 2);
+        float *mw = mid_ring + ((t + 1) & 1) * kZtbMidPlane;
+        load_col(xf, pf_);
+        if (has_margin) qf = pf_[mo];
+
+        // ---- first sweep, plane t+1 ----
+        if (t + 1 >= 0 && t + 1 < depth) {
+            sweep(full_tag, pc_ + own, xb, xc, xf, yf);
 #pragma unroll
-        for (int j = 0; j < kT3RPT; j++) {
-            if (live[j]) {
-                if (want) {
-                    const double d = fabs((double)v[j] - (double)yc[j]);
-                    if (d > dmax || d != d) dmax = d;
+            for (int k = 0; k < 4; k++) {
+                if (!FULL)
+                    yf[k] = pk2(live_row(full_tag, k) ? lo2(yf[k]) : 0.0f, live_row(full_tag, k + 4) ? hi2(yf[k]) : 0.0f);
+                mw[own_mid + k * P] = lo2(yf[k]);
+                mw[own_mid + (k + 4) * P] = hi2(yf[k]);
+            }
+            if (has_margin) {
+                const float *r = pc_ + mo;
+                const float sum = fn.sum7(r[-1], r[1], r[-P], r[P], qb, qf);
+                float v = div6_core(sum);
+                if (!__all_sync(0xFFFFFFFFu, !m_in || div6_in_range(sum)) && !div6_in_range(sum)) v = div6_cold(sum);
+                mw[mo_mid] = m_in ? v : 0.0f;
+            }
+        } else {  // outside the grid the intermediate plane is the neutral value
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                yf[k] = pk2(0.0f, 0.0f);
+                mw[own_mid + k * P] = 0.0f;
+                mw[own_mid + (k + 4) * P] = 0.0f;
+            }
+            if (has_margin) mw[mo_mid] = 0.0f;
+        }
+
+        // ---- second sweep, plane t ----
+        if (t >= zb) {
+            f32x2 v[4];
+            sweep(full_tag, mid_ring + (t & 1) * kZtbMidPlane + own_mid, yb, yc, yf, v);
+            float *o = out + ((size_t)t * rows + gy0) * cols + gx;
+#pragma unroll
+            for (int j = 0; j < kZtbRPT; j++) {
+                const float val = j < 4 ? lo2(v[j]) : hi2(v[j - 4]);
+                if (live_row(full_tag, j)) {
+                    if constexpr (WANT) {
+                        const float old = j < 4 ? lo2(yc[j]) : hi2(yc[j - 4]);
+                        const double d = fabs((double)val - (double)old);
+                        if (d > dmax || d != d) dmax = d;
+                    }
+                    o[(size_t)j * cols] = val;
                 }
-                o[(size_t)j * cols] = v[j];
             }
         }
-        const bool good = __syncthreads_and(t + 1 < ze ? wait_slot(next_in(s2)) : true);  // plane t+3 for step t+1
-        kin = s0;
-        kmid = m1;
-        return good;
+        bool good = true;
+        if (leader && t + 3 <= ze + 1) good = wait_plane(t + 3);  // read from step t+1 on
+        return __syncthreads_and(good);
     };
-    for (int t = zb; ok && t < ze; t += 3) {
-        ok = step(t, cc, ca, cb, mb, mc, ma);
-        if (ok && t + 1 < ze) ok = step(t + 1, ca, cb, cc, mc, ma, mb);
-        if (ok && t + 2 < ze) ok = step(t + 2, cb, cc, ca, ma, mb, mc);
+    auto march = [&](auto full_tag, auto want_tag) {
+        for (int t = zb - 2; ok && t < ze; t += 3) {
+            ok = step(full_tag, want_tag, t, ia, ib, ic, ma, mb, mc, pa, pc);
+            if (ok && t + 1 < ze) ok = step(full_tag, want_tag, t + 1, ib, ic, ia, mb, mc, ma, pb, pa);
+            if (ok && t + 2 < ze) ok = step(full_tag, want_tag, t + 2, ic, ia, ib, mc, ma, mb, pc, pb);
+        }
+    };
+    // one march per case, so that the common one (every strip cell inside,
+    // no residual) carries no tests it does not need
+    if (full) {
+        if (want) march(std::true_type{}, std::true_type{});
+        else march(std::true_type{}, std::false_type{});
+    } else {
+        if (want) march(std::false_type{}, std::true_type{});
+        else march(std::false_type{}, std::false_type{});
     }
-    if (!ok && threadIdx.x == 0) {
-        // let loads still in flight land before the CTA gives up its shared memory
-        for (int k = 0; k < kZtbIn; k++)
-            if (pending & (1u << k)) mbar_poll(&bar[k], (phase >> k) & 1u, kMaxWaitPolls);
-    }
+    if (!ok && leader) drain();
     if (want) {
         dmax = block_max(dmax);
         if (threadIdx.x == 0) atomic_max_nonneg(resid, dmax);
     }
 }
 
-// Two sweeps in -> out of a kStar7 functor with neutral +0 on FP32 cells;
-// cudaErrorNotSupported when the grid does not suit the kernel.
+// z planes per CTA: the longest chunk (24 planes down to 4) that still gives
+// at least two waves of resident CTAs. Longer chunks spend less on the first
+// sweep's two extra planes and the march's start; on heat3D 512^3 (128 tiles,
+// 456 resident CTAs) 24 planes measured best (11.7 ms per 100 sweeps against
+// 12.0 for 16 and 11.8 for 32).
+inline int stencil3d_ztb_zchunk(int depth, long long tiles, long long resident) {
+    static const int kCand[] = {24, 16, 12, 8, 6, 4};
+    for (int z : kCand)
+        if (tiles * ((depth + z - 1) / z) >= 2 * resident) return z;
+    return 4;
+}
+
+// Two sweeps in -> out of a kSum7Div6 functor with neutral +0 on FP32 cells;
+// cudaErrorNotSupported when the grid does not suit the kernel. zchunk 0
+// picks the chunk length.
 template <class Fn>
 cudaError_t launch_stencil3d_ztb(const float *in, float *out, int depth, int rows, int cols, Fn fn,
-                                 unsigned long long *resid, unsigned *err, cudaStream_t st) {
-    if (!stencil_tma_ok<float>(in, cols, kZtbPitch, kZtbRows)) return cudaErrorNotSupported;
+                                 unsigned long long *resid, unsigned *err, cudaStream_t st, int zchunk = 0) {
+    if (!stencil_tma_ok<float>(in, cols, kZtbPitch, kZtbRows) || ((uintptr_t)out % 16) != 0)
+        return cudaErrorNotSupported;
     CUtensorMap map{};
     cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)depth};
     cuuint64_t strides[2] = {(cuuint64_t)cols * sizeof(float), (cuuint64_t)cols * rows * sizeof(float)};
@@ -294,8 +380,19 @@ cudaError_t launch_stencil3d_ztb(const float *in, float *out, int depth, int row
     const size_t smem = stencil3d_ztb_smem();
     auto k = stencil3d_ztb_kernel<Fn>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((cols + kT3BX - 1) / kT3BX, (rows + kT3BY - 1) / kT3BY, (depth + kZtbChunk - 1) / kZtbChunk);
-    k<<<grid, kT3Threads, smem, st>>>(map, out, depth, rows, cols, fn, resid, err);
+    static int per_sm = 0, sms = 0;  // per instantiation
+    if (per_sm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kZtbThreads, smem);
+        if (per_sm < 1) per_sm = 1;
+    }
+    const long long tiles = (long long)((cols + kZtbBX - 1) / kZtbBX) * ((rows + kZtbBY - 1) / kZtbBY);
+    const int zc = zchunk > 0 ? zchunk : stencil3d_ztb_zchunk(depth, tiles, (long long)per_sm * sms);
+    const long long blocks = tiles * ((depth + zc - 1) / zc);
+    if (blocks > 0x7FFFFFFFLL) return cudaErrorNotSupported;
+    k<<<(unsigned)blocks, kZtbThreads, smem, st>>>(map, out, depth, rows, cols, zc, fn, resid, err);
     return cudaGetLastError();
 }
 

@@ -59,7 +59,9 @@ def test_setters_validate_their_arguments(lib):
     assert lib.msl_set_temporal_depth(33) == bad and lib.msl_set_temporal_depth(-1) == bad
     assert lib.msl_set_temporal_depth(32) == abi.MSL_OK and lib.msl_set_temporal_depth(0) == abi.MSL_OK
     assert lib.msl_set_stencil3d_depth(0) == bad and lib.msl_set_stencil3d_depth(3) == bad
-    assert lib.msl_set_stencil3d_depth(2) == abi.MSL_OK and lib.msl_set_stencil3d_depth(1) == abi.MSL_OK
+    assert lib.msl_set_stencil3d_depth(1) == abi.MSL_OK and lib.msl_set_stencil3d_depth(2) == abi.MSL_OK
+    assert lib.msl_set_stencil3d_zchunk(-1) == bad and lib.msl_set_stencil3d_zchunk(1025) == bad
+    assert lib.msl_set_stencil3d_zchunk(1) == abi.MSL_OK and lib.msl_set_stencil3d_zchunk(0) == abi.MSL_OK
     assert lib.msl_set_stencil3d_persistent(2) == bad and lib.msl_set_stencil3d_persistent(-2) == bad
     assert lib.msl_set_stencil3d_persistent(-1) == abi.MSL_OK
     assert lib.msl_set_tma(0) == abi.MSL_OK and lib.msl_set_tma(1) == abi.MSL_OK

@@ -99,11 +99,24 @@ def test_life_8192_200_steps(gpu, life_8192, depth):
     assert np.array_equal(last.download(), want)
 
 
-def test_heat3d_512_100_steps(gpu):
+@pytest.fixture(scope="module")
+def heat512():
     cube = W.heat_cube(512, 512, 512, 42)
-    a, b = gpu.DeviceArray.from_host(cube), gpu.DeviceArray(cube.shape, np.float32)
-    last, res = gpu.stencil3d_iterate(gpu.MSL_ST3_HEAT7, a, b, 1, 0.0, 100)
-    want, _, want_res = O.stencil3d_iterate(gpu.MSL_ST3_HEAT7, cube, 1, 0.0, 100)
+    want, _, want_res = O.stencil3d_iterate(A.MSL_ST3_HEAT7, cube, 1, 0.0, 100)
+    return cube, want, want_res
+
+
+@pytest.mark.parametrize("sweeps_per_launch", [2, 1])
+def test_heat3d_512_100_steps(gpu, heat512, sweeps_per_launch):
+    """Both heat3D paths at full size: two sweeps per launch (the z-marching
+    kernel, the default) and one."""
+    cube, want, want_res = heat512
+    gpu.set_stencil3d_depth(sweeps_per_launch)
+    try:
+        a, b = gpu.DeviceArray.from_host(cube), gpu.DeviceArray(cube.shape, np.float32)
+        last, res = gpu.stencil3d_iterate(gpu.MSL_ST3_HEAT7, a, b, 1, 0.0, 100)
+    finally:
+        gpu.set_stencil3d_depth(2)
     assert np.array_equal(last.download(), want)
     assert res == want_res
 

@@ -380,7 +380,25 @@ def test_stencil3d_heat_z_marching(gpu, shape, sweeps_per_launch):
             assert bits_equal(last.download(), want), iters
             assert res == want_res, iters
     finally:
-        gpu.set_stencil3d_depth(1)
+        gpu.set_stencil3d_depth(2)
+
+
+@pytest.mark.parametrize("zchunk", [1, 2, 3, 7, 24, 0])
+def test_stencil3d_heat_z_chunks(gpu, zchunk):
+    """The z-marching kernel's result does not depend on how the depth is cut
+    into per-CTA chunks (1 plane per CTA up to the whole depth; 0 = chosen per
+    grid): 4 sweeps with the residual against the oracle."""
+    x = W.heat_cube(40, 70, 68, seed=9)
+    want, _, want_res = O.stencil3d_iterate(gpu.MSL_ST3_HEAT7, x, 1, 0.0, 4)
+    gpu.set_stencil3d_depth(2)
+    gpu.set_stencil3d_zchunk(zchunk)
+    try:
+        a, b = dev(gpu, x), gpu.DeviceArray(x.shape, x.dtype)
+        last, res = gpu.stencil3d_iterate(gpu.MSL_ST3_HEAT7, a, b, 1, 0.0, 4)
+    finally:
+        gpu.set_stencil3d_zchunk(0)
+    assert bits_equal(last.download(), want)
+    assert res == want_res
 
 
 @pytest.mark.parametrize("sweeps_per_launch", [2, 1])
@@ -404,7 +422,7 @@ def test_stencil3d_heat_special_values(gpu, sweeps_per_launch):
             want = O.stencil3d_iterate(gpu.MSL_ST3_HEAT7, x, 1, 0.0, iters)[0]
             assert bits_equal(last.download(), want), iters
     finally:
-        gpu.set_stencil3d_depth(1)
+        gpu.set_stencil3d_depth(2)
 
 
 @pytest.mark.parametrize("persistent", [0, 1])
