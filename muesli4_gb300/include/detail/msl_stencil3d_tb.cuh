@@ -14,10 +14,13 @@
 // plus two cells on every side, x rounded out to 16 bytes) arrive by TMA in a
 // ring of four slots, issued two steps before their first use.
 //
-// Every thread owns one column of eight vertically adjacent cells and keeps
-// its input and intermediate values of the three planes a star reads in
-// registers (B, centre and F of both sweeps; N and S inside the strip); W, E
-// and the strip's two ends come from shared memory. The margin lanes keep
+// Every thread owns a strip of two adjacent columns by four rows, kept as
+// four packed pairs (one per row), and holds its input and intermediate values
+// of the three planes a star reads in registers (B, centre and F of both
+// sweeps; N and S inside the strip; W of the right column and E of the left).
+// The pairs move between registers and shared memory as 64-bit accesses; only
+// the strip's outer W and E cells and its two end rows come from shared
+// memory cell by cell or pair by pair. The margin lanes keep
 // their input values in registers the same way, so no step reads an input
 // plane older than t+1 and the slot of plane t takes the load of plane t+4 as
 // the step begins. The roles of the register columns rotate with the plane:
@@ -32,7 +35,8 @@
 // Requirements (checked by the launcher): FP32 cells, a functor with
 // kSum7Div6 (heat3D), neutral value +0 -- outside the grid both the staged
 // input (TMA zero fill) and the intermediate sweep (set explicitly) hold 0,
-// which is exactly the view's neutral value -- and a grid TMA can address.
+// which is exactly the view's neutral value -- a grid TMA can address and an
+// output 16-byte aligned (rows are then 8-byte aligned for the pair stores).
 // Results are bit-identical to two launches of the one-sweep kernel: every
 // cell of every sweep is computed by the same functor from the same operands;
 // only where the operands live differs.
@@ -43,7 +47,7 @@
 namespace msl {
 namespace gpu {
 
-constexpr int kZtbBX = 64, kZtbBY = 32, kZtbRPT = 8, kZtbThreads = 256;
+constexpr int kZtbBX = 64, kZtbBY = 32, kZtbRPT = 4, kZtbThreads = 256;
 constexpr int kZtbPitch = kZtbBX + 8;                    // 72: window x0-4 .. x0+67
 constexpr int kZtbRows = kZtbBY + 4;                     // 36: window y0-2 .. y0+33
 constexpr int kZtbPlane = kZtbPitch * kZtbRows;          // floats per input slot (10368 bytes = 81 x 128)
@@ -61,9 +65,9 @@ template <class Fn, class = void> struct IsSum7Div6 : std::false_type {};
 template <class Fn> struct IsSum7Div6<Fn, std::void_t<decltype(Fn::kSum7Div6)>> : std::bool_constant<Fn::kSum7Div6> {};
 
 // Packed FP32 pairs (add/mul/fma.rn.f32x2: two independent IEEE operations
-// per instruction, each rounded as the scalar one). A thread's strip keeps
-// cells j and j+4 in one pair, so the N and S operands of a pair are again
-// pairs of the strip (all but the strip's two ends).
+// per instruction, each rounded as the scalar one). A pair is two cells of a
+// row, x and x+1: the B, F, N and S operands of a pair are pairs of the same
+// two columns, W and E pairs take one cell from the neighbouring column.
 using f32x2 = unsigned long long;
 MSL_DEV f32x2 pk2(float a, float b) {
     f32x2 d;
@@ -112,6 +116,27 @@ MSL_DEV f32x2 div6_core2(f32x2 x) {
     const f32x2 r = fma2(q, pk2(-6.0f, -6.0f), x);
     return fma2(r, z2, q);
 }
+// True when all eight halves of the strip's four pairs lie in the division's
+// fast-path range 2^-122 <= |x| <= FLT_MAX: one predicate chained through the
+// comparisons (NaN compares false).
+MSL_DEV bool strip_in_range(const f32x2 (&v)[4]) {
+    unsigned r;
+    asm("{\n\t.reg .pred p;\n\t.reg .f32 a0, a1, a2, a3, a4, a5, a6, a7;\n\t"
+        "mov.b64 {a0, a1}, %1;\n\tmov.b64 {a2, a3}, %2;\n\tmov.b64 {a4, a5}, %3;\n\tmov.b64 {a6, a7}, %4;\n\t"
+        "abs.f32 a0, a0;\n\tabs.f32 a1, a1;\n\tabs.f32 a2, a2;\n\tabs.f32 a3, a3;\n\t"
+        "abs.f32 a4, a4;\n\tabs.f32 a5, a5;\n\tabs.f32 a6, a6;\n\tabs.f32 a7, a7;\n\t"
+        "setp.ge.f32 p, a0, 0f02800000;\n\tsetp.le.and.f32 p, a0, 0f7F7FFFFF, p;\n\t"
+        "setp.ge.and.f32 p, a1, 0f02800000, p;\n\tsetp.le.and.f32 p, a1, 0f7F7FFFFF, p;\n\t"
+        "setp.ge.and.f32 p, a2, 0f02800000, p;\n\tsetp.le.and.f32 p, a2, 0f7F7FFFFF, p;\n\t"
+        "setp.ge.and.f32 p, a3, 0f02800000, p;\n\tsetp.le.and.f32 p, a3, 0f7F7FFFFF, p;\n\t"
+        "setp.ge.and.f32 p, a4, 0f02800000, p;\n\tsetp.le.and.f32 p, a4, 0f7F7FFFFF, p;\n\t"
+        "setp.ge.and.f32 p, a5, 0f02800000, p;\n\tsetp.le.and.f32 p, a5, 0f7F7FFFFF, p;\n\t"
+        "setp.ge.and.f32 p, a6, 0f02800000, p;\n\tsetp.le.and.f32 p, a6, 0f7F7FFFFF, p;\n\t"
+        "setp.ge.and.f32 p, a7, 0f02800000, p;\n\tsetp.le.and.f32 p, a7, 0f7F7FFFFF, p;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r) : "l"(v[0]), "l"(v[1]), "l"(v[2]), "l"(v[3]));
+    return r != 0;
+}
 // IEEE-correct x / 6 for sums outside the fast path's range; out of line so
 // that the rare path does not crowd the march's instruction cache.
 static __device__ __noinline__ float div6_cold(float x) { return div6_rn(x); }
@@ -137,7 +162,7 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
     stencil3d_ztb_kernel(const __grid_constant__ CUtensorMap tmap, float *out, int depth, int rows, int cols,
                          int zchunk, Fn fn, unsigned long long *resid, unsigned *err) {
     static_assert(IsSum7Div6<Fn>::value, "the two-sweep kernel takes sum7 / 6 functors");
-    static_assert(kZtbRPT == 8, "cells j and j+4 of the strip form a pair");
+    static_assert(kZtbRPT == 4 && kZtbBY == 8 * kZtbRPT, "eight warps of 64 x 4 cells");
     constexpr int P = kZtbPitch;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);  // one mbarrier per input slot
@@ -157,8 +182,8 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
     // warp, which has no margin item
     const bool leader = threadIdx.x == kZtbThreads - 32;
 
-    // this thread's strip: window column cx, rows cy .. cy+7
-    const int cx = 4 + (warp & 1) * 32 + lane, cy = 2 + (warp >> 1) * kZtbRPT;
+    // this thread's strip: window columns cx, cx+1 (8-byte aligned), rows cy .. cy+3
+    const int cx = 4 + 2 * lane, cy = 2 + warp * kZtbRPT;
     const int gx = wx0 + cx, gy0 = wy0 + cy;
     const int own = cy * P + cx, own_mid = own - P;  // intermediate slots start at window row 1
     const bool x_in = gx < cols;
@@ -221,10 +246,10 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
         return;
     }
 
-    // register columns, pair k = cells k and k+4 of the strip
+    // register columns, pair k = row k of the strip
     auto load_col = [&](f32x2 (&d)[4], const float *plane) {
 #pragma unroll
-        for (int k = 0; k < 4; k++) d[k] = pk2(plane[own + k * P], plane[own + (k + 4) * P]);
+        for (int k = 0; k < 4; k++) d[k] = *reinterpret_cast<const f32x2 *>(plane + own + k * P);
     };
     f32x2 ia[4], ib[4], ic[4];  // input columns
     f32x2 ma[4], mb[4], mc[4];  // intermediate columns
@@ -249,18 +274,19 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
     // the four pairs' sums, then x / 6.
     auto sweep = [&](auto full_tag, const float *q, const f32x2 (&cb)[4], const f32x2 (&cc)[4],
                      const f32x2 (&cf)[4], f32x2 (&v)[4]) {
-        const float n = q[-P], s = q[kZtbRPT * P];
+        const f32x2 n = *reinterpret_cast<const f32x2 *>(q - P), s = *reinterpret_cast<const f32x2 *>(q + kZtbRPT * P);
         bool good = true;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            const f32x2 w = pk2(q[k * P - 1], q[(k + 4) * P - 1]);
-            const f32x2 e = pk2(q[k * P + 1], q[(k + 4) * P + 1]);
-            const f32x2 nn = k == 0 ? pk2(n, lo2(cc[3])) : cc[k - 1];
-            const f32x2 ss = k == 3 ? pk2(hi2(cc[0]), s) : cc[k + 1];
+            const f32x2 w = pk2(q[k * P - 1], lo2(cc[k]));
+            const f32x2 e = pk2(hi2(cc[k]), q[k * P + 2]);
+            const f32x2 nn = k == 0 ? n : cc[k - 1];
+            const f32x2 ss = k == 3 ? s : cc[k + 1];
             v[k] = sum7x2(w, e, nn, ss, cb[k], cf[k]);
-            good = good && (!live_row(full_tag, k) || div6_in_range(lo2(v[k])));
-            good = good && (!live_row(full_tag, k + 4) || div6_in_range(hi2(v[k])));
+            if constexpr (!decltype(full_tag)::value)
+                good = good && (!live_row(full_tag, k) || (div6_in_range(lo2(v[k])) && div6_in_range(hi2(v[k]))));
         }
+        if constexpr (decltype(full_tag)::value) good = strip_in_range(v);
         div6_pairs(good, v);
     };
     // Step t: intermediate plane t+1 (from input planes t, t+1, t+2), then
@@ -281,10 +307,8 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
             sweep(full_tag, pc_ + own, xb, xc, xf, yf);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                if (!FULL)
-                    yf[k] = pk2(live_row(full_tag, k) ? lo2(yf[k]) : 0.0f, live_row(full_tag, k + 4) ? hi2(yf[k]) : 0.0f);
-                mw[own_mid + k * P] = lo2(yf[k]);
-                mw[own_mid + (k + 4) * P] = hi2(yf[k]);
+                if (!FULL && !live_row(full_tag, k)) yf[k] = pk2(0.0f, 0.0f);
+                *reinterpret_cast<f32x2 *>(mw + own_mid + k * P) = yf[k];
             }
             if (has_margin) {
                 const float *r = pc_ + mo;
@@ -297,8 +321,7 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 yf[k] = pk2(0.0f, 0.0f);
-                mw[own_mid + k * P] = 0.0f;
-                mw[own_mid + (k + 4) * P] = 0.0f;
+                *reinterpret_cast<f32x2 *>(mw + own_mid + k * P) = yf[k];
             }
             if (has_margin) mw[mo_mid] = 0.0f;
         }
@@ -309,15 +332,15 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
             sweep(full_tag, mid_ring + (t & 1) * kZtbMidPlane + own_mid, yb, yc, yf, v);
             float *o = out + ((size_t)t * rows + gy0) * cols + gx;
 #pragma unroll
-            for (int j = 0; j < kZtbRPT; j++) {
-                const float val = j < 4 ? lo2(v[j]) : hi2(v[j - 4]);
-                if (live_row(full_tag, j)) {
+            for (int k = 0; k < kZtbRPT; k++) {
+                if (live_row(full_tag, k)) {
                     if constexpr (WANT) {
-                        const float old = j < 4 ? lo2(yc[j]) : hi2(yc[j - 4]);
-                        const double d = fabs((double)val - (double)old);
-                        if (d > dmax || d != d) dmax = d;
+                        const double d0 = fabs((double)lo2(v[k]) - (double)lo2(yc[k]));
+                        const double d1 = fabs((double)hi2(v[k]) - (double)hi2(yc[k]));
+                        if (d0 > dmax || d0 != d0) dmax = d0;
+                        if (d1 > dmax || d1 != d1) dmax = d1;
                     }
-                    o[(size_t)j * cols] = val;
+                    *reinterpret_cast<f32x2 *>(o + (size_t)k * cols) = v[k];
                 }
             }
         }
