@@ -39,6 +39,7 @@ template <typename T> struct StHeat5 {
 template <typename T> struct StJacobi5 {
     static constexpr bool kStrip2 = true;
     static constexpr bool kStripAnyTile = true;  // strip() reads the window only and handles the edges
+    static constexpr bool kPairStrip = std::is_same<T, float>::value;  // packed pairs (jacobi_pair_strip)
     template <class V> __device__ __forceinline__ T operator()(const V &m, int x, int y) const {
         if (x == 0 || y == 0 || x == m.width - 1 || y == m.height - 1) return m(x, y);
         return heat5<T>(m, x, y);

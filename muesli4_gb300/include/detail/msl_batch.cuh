@@ -89,6 +89,7 @@ MSL_DEV void batch_finalize_body(BatchGrid *grids, const int *list, int nlist, i
 struct JacobiFn {
     static constexpr bool kStrip2 = true;
     static constexpr bool kStripAnyTile = true;  // strip() reads the window only and handles the edges
+    static constexpr bool kPairStrip = true;     // FP32 grids: packed pairs (jacobi_pair_strip)
     template <class V, typename T> __device__ __forceinline__ void strip(const V &m, int x, int y0, T (&out)[kSt2RPT]) const {
         jacobi_strip_window(m, x, y0, out);
     }
@@ -291,7 +292,10 @@ __global__ void __launch_bounds__(kSt2Threads)
         const int x = x0 + (warp % (kSt2BX / 32)) * 32 + lane;
         const int ys = y0 + (warp / (kSt2BX / 32)) * kSt2RPT;
         double dmax = 0.0;
-        if (x0 - r >= 0 && y0 - r >= 0 && x0 + kSt2BX + r <= cols && y0 + kSt2BY + r <= rows) {
+        if constexpr (has_pair_strip<std::remove_cv_t<decltype(fn)>>::value && std::is_same<S, float>::value) {
+            jacobi_pair_block(reinterpret_cast<const float *>(m.tile_), pitch, wx0, wy0, x0, y0, rows, cols,
+                              reinterpret_cast<float *>(out), check != 0, dmax);
+        } else if (x0 - r >= 0 && y0 - r >= 0 && x0 + kSt2BX + r <= cols && y0 + kSt2BY + r <= rows) {
             m.check_ = false;
             stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, check != 0, dmax);
         } else {

@@ -246,6 +246,43 @@ template <typename T> MSL_DEV T shfl_down(T v, int delta, int width = 32) {
 namespace msl {
 namespace gpu {
 
+// Packed FP32 pairs (add/mul/fma.rn.f32x2, sm_100 and later: two independent
+// IEEE operations per instruction, each rounded as the scalar one; the low
+// half is the first float). The stencil kernels pair two cells of a row.
+using f32x2 = unsigned long long;
+MSL_DEV f32x2 pk2(float a, float b) {
+    f32x2 d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(a), "f"(b));
+    return d;
+}
+MSL_DEV float lo2(f32x2 v) {
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return a;
+}
+MSL_DEV float hi2(f32x2 v) {
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return b;
+}
+MSL_DEV f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+MSL_DEV f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+MSL_DEV f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+MSL_DEV f32x2 ld_pair(const float *p) { return *reinterpret_cast<const f32x2 *>(p); }  // 8-byte aligned
+MSL_DEV void st_pair(float *p, f32x2 v) { *reinterpret_cast<f32x2 *>(p) = v; }
+
 // x / 6 rounded to nearest, via the reciprocal-with-one-correction method for
 // a divisor known in advance (P. Markstein, "IA-64 and Elementary Functions",
 // 2000; N. Brisebarre, J.-M. Muller, S. K. Raina, "Accelerating correctly

@@ -250,6 +250,79 @@ template <class V, typename T> MSL_DEV void jacobi_strip_window(const V &m, int 
     }
 }
 
+// Functors that are plain Jacobi on FP32 cells may declare kPairStrip: the
+// temporal-blocking sweeps then run jacobi_pair_strip on packed pairs of
+// columns instead of strip() column by column (same values, bit for bit).
+template <class F, class = void> struct has_pair_strip : std::false_type {};
+template <class F>
+struct has_pair_strip<F, std::void_t<decltype(F::kPairStrip)>> : std::bool_constant<F::kPairStrip> {};
+constexpr int kPairRows = 4;
+
+// Plain Jacobi for the cells (x, y0 + k) and (x + 1, y0 + k), k < kPairRows,
+// read from the window only (p: the window address of (x, y0), 8-byte
+// aligned; rows pitch apart): heat2D of the four neighbours, (((0 + W) + E) +
+// N) + S times 0.25, two cells per add.rn/mul.rn.f32x2; then cells on the
+// grid's edge -- and cells outside the grid, which are never stored -- keep
+// their value, as jacobi_strip_window computes them one by one. c returns the
+// cells' previous values.
+MSL_DEV void jacobi_pair_strip(const float *p, int pitch, int x, int y0, int cols, int rows,
+                               f32x2 (&c)[kPairRows], f32x2 (&v)[kPairRows]) {
+    const f32x2 n = ld_pair(p - pitch), s = ld_pair(p + kPairRows * pitch);
+#pragma unroll
+    for (int k = 0; k < kPairRows; k++) c[k] = ld_pair(p + k * pitch);
+#pragma unroll
+    for (int k = 0; k < kPairRows; k++) {
+        const f32x2 w = pk2(p[k * pitch - 1], lo2(c[k]));
+        const f32x2 e = pk2(hi2(c[k]), p[k * pitch + 2]);
+        f32x2 t = add2(pk2(0.0f, 0.0f), w);
+        t = add2(t, e);
+        t = add2(t, k == 0 ? n : c[k - 1]);
+        t = add2(t, k == kPairRows - 1 ? s : c[k + 1]);
+        v[k] = mul2(t, pk2(0.25f, 0.25f));
+    }
+    if (x >= 1 && x + 2 <= cols - 1 && y0 >= 1 && y0 + kPairRows <= rows - 1) return;  // no edge cell
+    const bool xb0 = x <= 0 || x >= cols - 1, xb1 = x + 1 <= 0 || x + 1 >= cols - 1;
+#pragma unroll
+    for (int k = 0; k < kPairRows; k++) {
+        const int y = y0 + k;
+        const bool yb = y <= 0 || y >= rows - 1;
+        v[k] = pk2((xb0 || yb) ? lo2(c[k]) : lo2(v[k]), (xb1 || yb) ? hi2(c[k]) : hi2(v[k]));
+    }
+}
+
+// The sweep of a 64 x (kPairRows * warps) block to global memory on packed
+// pairs: thread t owns columns x0 + 2 (t % 32) and the next, rows y0 +
+// kPairRows (t / 32) onwards. win: the window holding the sweep's input
+// (origin wx0, wy0). With want, the FP64 max |new - old| of the stored cells
+// into dmax.
+MSL_DEV void jacobi_pair_block(const float *win, int pitch, int wx0, int wy0, int x0, int y0, int rows, int cols,
+                               float *out, bool want, double &dmax) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x = x0 + 2 * lane, y = y0 + kPairRows * warp;
+    f32x2 c[kPairRows], v[kPairRows];
+    jacobi_pair_strip(win + (y - wy0) * pitch + (x - wx0), pitch, x, y, cols, rows, c, v);
+    const bool pairs = (cols & 1) == 0 && ((uintptr_t)out & 7) == 0 && x + 1 < cols;
+#pragma unroll
+    for (int k = 0; k < kPairRows; k++) {
+        if (y + k >= rows || x >= cols) break;
+        float *o = out + (size_t)(y + k) * cols + x;
+        if (want) {
+            const double d0 = fabs((double)lo2(v[k]) - (double)lo2(c[k]));
+            if (d0 > dmax || d0 != d0) dmax = d0;
+            if (x + 1 < cols) {
+                const double d1 = fabs((double)hi2(v[k]) - (double)hi2(c[k]));
+                if (d1 > dmax || d1 != d1) dmax = d1;
+            }
+        }
+        if (pairs) {
+            st_pair(o, v[k]);
+        } else {
+            o[0] = lo2(v[k]);
+            if (x + 1 < cols) o[1] = hi2(v[k]);
+        }
+    }
+}
+
 MSL_DEV void atomic_max_nonneg(unsigned long long *slot, double v) {
     atomicMax(slot, (unsigned long long)__double_as_longlong(v));
 }
@@ -338,7 +411,28 @@ MSL_DEV void tb_inner_sweeps(const Fn &fn, NPLMatrix<typename Compute<S>::type, 
                 }
             }
         };
-        if (interior || has_any_tile_strip<Fn>::value) {
+        if constexpr (has_pair_strip<Fn>::value && std::is_same<S, float>::value) {
+            // Packed pairs (FP32 Jacobi): the region as a list of 2-column x
+            // kPairRows-row strips at even window columns (hx is a multiple of
+            // 4, so the pair accesses are 8-byte aligned); the strips start
+            // every kPairRows rows, the last one moved up to end at row H (two
+            // threads then write the same values). A side range of odd width
+            // takes one more column outside the region, whose value no cell
+            // that a later sweep needs reads; its reads stay inside the buffer.
+            const int ext_e = (ext + 1) & ~1;
+            const int npairs = kSt2BX / 2 + ext_e, ns = (H + kPairRows - 1) / kPairRows;
+            const int wc0 = x0 - wx0 - ext_e, wr0 = gy0 - wy0;
+            const float *src = reinterpret_cast<const float *>(m.tile_);
+            float *d = reinterpret_cast<float *>(dst);
+            for (int it = threadIdx.x; it < ns * npairs; it += blockDim.x) {
+                const int sr = it / npairs, pc = it - sr * npairs;
+                const int wc = wc0 + 2 * pc, wr = wr0 + min(sr * kPairRows, H - kPairRows);
+                f32x2 c[kPairRows], v[kPairRows];
+                jacobi_pair_strip(src + wr * pitch + wc, pitch, wx0 + wc, wy0 + wr, cols, rows, c, v);
+#pragma unroll
+                for (int k = 0; k < kPairRows; k++) st_pair(d + (wr + k) * pitch + wc, v[k]);
+            }
+        } else if (interior || has_any_tile_strip<Fn>::value) {
             m.check_ = false;
             if constexpr (has_strip2<Fn>::value) {
                 // Whole kSt2RPT-row strips through the functor's strip(): the
@@ -427,7 +521,11 @@ __global__ void __launch_bounds__(kSt2Threads)
     const bool interior = wx0 >= 0 && wy0 >= 0 && wx0 + pitch <= cols && wy0 + th <= rows;
     const bool want = resid != nullptr;
     double dmax = 0.0;
-    if (interior) {
+    if constexpr (has_pair_strip<Fn>::value && std::is_same<S, float>::value) {
+        static_assert(kSt2Threads == 32 * (kSt2BY / kPairRows), "one pair strip per thread");
+        jacobi_pair_block(reinterpret_cast<const float *>(tile), pitch, wx0, wy0, x0, y0, rows, cols,
+                          reinterpret_cast<float *>(out), want, dmax);
+    } else if (interior) {
         m.check_ = false;
         stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, want, dmax);
     } else {
@@ -498,7 +596,11 @@ __global__ void __launch_bounds__(BY * 8)
     const bool interior = x0 - r >= 0 && y0 - r >= 0 && x0 + kSt2BX + r <= cols && y0 + BY + r <= rows;
     const bool want = resid != nullptr;
     double dmax = 0.0;
-    if (interior) {
+    if constexpr (has_pair_strip<Fn>::value && std::is_same<S, float>::value) {
+        static_assert(BY * 8 == 32 * (BY / kPairRows), "one pair strip per thread");
+        jacobi_pair_block(reinterpret_cast<const float *>(m.tile_), pitch, wx0, wy0, x0, y0, rows, cols,
+                          reinterpret_cast<float *>(out), want, dmax);
+    } else if (interior) {
         m.check_ = false;
         stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, want, dmax);
     } else {

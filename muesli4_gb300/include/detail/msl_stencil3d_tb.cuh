@@ -64,41 +64,6 @@ inline size_t stencil3d_ztb_smem() {
 template <class Fn, class = void> struct IsSum7Div6 : std::false_type {};
 template <class Fn> struct IsSum7Div6<Fn, std::void_t<decltype(Fn::kSum7Div6)>> : std::bool_constant<Fn::kSum7Div6> {};
 
-// Packed FP32 pairs (add/mul/fma.rn.f32x2: two independent IEEE operations
-// per instruction, each rounded as the scalar one). A pair is two cells of a
-// row, x and x+1: the B, F, N and S operands of a pair are pairs of the same
-// two columns, W and E pairs take one cell from the neighbouring column.
-using f32x2 = unsigned long long;
-MSL_DEV f32x2 pk2(float a, float b) {
-    f32x2 d;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(a), "f"(b));
-    return d;
-}
-MSL_DEV float lo2(f32x2 v) {
-    float a, b;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-    return a;
-}
-MSL_DEV float hi2(f32x2 v) {
-    float a, b;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-    return b;
-}
-MSL_DEV f32x2 add2(f32x2 a, f32x2 b) {
-    f32x2 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-MSL_DEV f32x2 mul2(f32x2 a, f32x2 b) {
-    f32x2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-MSL_DEV f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
-    f32x2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
 // heat3D's sum of six neighbours in its order, (((((0 + w) + e) + n) + s) + b) + f, for a pair.
 MSL_DEV f32x2 sum7x2(f32x2 w, f32x2 e, f32x2 n, f32x2 s, f32x2 b, f32x2 f) {
     f32x2 v = add2(pk2(0.0f, 0.0f), w);
@@ -249,7 +214,7 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
     // register columns, pair k = row k of the strip
     auto load_col = [&](f32x2 (&d)[4], const float *plane) {
 #pragma unroll
-        for (int k = 0; k < 4; k++) d[k] = *reinterpret_cast<const f32x2 *>(plane + own + k * P);
+        for (int k = 0; k < 4; k++) d[k] = ld_pair(plane + own + k * P);
     };
     f32x2 ia[4], ib[4], ic[4];  // input columns
     f32x2 ma[4], mb[4], mc[4];  // intermediate columns
@@ -274,7 +239,7 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
     // the four pairs' sums, then x / 6.
     auto sweep = [&](auto full_tag, const float *q, const f32x2 (&cb)[4], const f32x2 (&cc)[4],
                      const f32x2 (&cf)[4], f32x2 (&v)[4]) {
-        const f32x2 n = *reinterpret_cast<const f32x2 *>(q - P), s = *reinterpret_cast<const f32x2 *>(q + kZtbRPT * P);
+        const f32x2 n = ld_pair(q - P), s = ld_pair(q + kZtbRPT * P);
         bool good = true;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
@@ -308,7 +273,7 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 if (!FULL && !live_row(full_tag, k)) yf[k] = pk2(0.0f, 0.0f);
-                *reinterpret_cast<f32x2 *>(mw + own_mid + k * P) = yf[k];
+                st_pair(mw + own_mid + k * P, yf[k]);
             }
             if (has_margin) {
                 const float *r = pc_ + mo;
@@ -321,7 +286,7 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 yf[k] = pk2(0.0f, 0.0f);
-                *reinterpret_cast<f32x2 *>(mw + own_mid + k * P) = yf[k];
+                st_pair(mw + own_mid + k * P, yf[k]);
             }
             if (has_margin) mw[mo_mid] = 0.0f;
         }
@@ -340,7 +305,7 @@ __global__ void __launch_bounds__(kZtbThreads, MSL_ZTB_MIN_CTAS)
                         if (d0 > dmax || d0 != d0) dmax = d0;
                         if (d1 > dmax || d1 != d1) dmax = d1;
                     }
-                    *reinterpret_cast<f32x2 *>(o + (size_t)k * cols) = v[k];
+                    st_pair(o + (size_t)k * cols, v[k]);
                 }
             }
         }
