@@ -407,7 +407,7 @@ class Jacobi:
         self.h2d, self.d2h = h.nbytes, h.nbytes + 8
         self.residual = None
         d = getattr(self, "fixed_depth", 0)
-        rows = 32
+        rows = getattr(self, "fixed_tile_rows", 0) or 32
         if d <= 0:
             d, rows, _ = A.autotune_stencil2d_shape(A.MSL_ST2_JACOBI5, A.MSL_F32, self.side, self.side, 1, 64)
         tiles = ((self.side + 63) // 64) * ((self.side + rows - 1) // rows)
@@ -965,6 +965,8 @@ def main():
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[0.25, 0.5, 1.0, 2.0])
     ap.add_argument("--temporal-depth", type=int, default=0,
                     help="sweeps per launch of the iterated 2-D stencils (0: the autotuner's choice)")
+    ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 16, 32, 64],
+                    help="tile height of the 2-D temporal-blocking kernel with --temporal-depth (0: 32)")
     ap.add_argument("--stencil3d-depth", type=int, default=2, choices=[1, 2],
                     help="heat3D sweeps per launch: 2 the z-marching kernel (default), 1 one sweep")
     ap.add_argument("--stencil3d-persistent", type=int, default=-1, choices=[-1, 0, 1],
@@ -996,10 +998,13 @@ def main():
     w = MapZipFold(A, args.elements) if args.workload == "mapzipfold" and args.elements > 0 \
         else WORKLOADS[args.workload](A)
     w.fixed_depth = args.temporal_depth  # > 0: no autotuning of the Life depth
+    w.fixed_tile_rows = args.tile_rows
     w.heat_sweeps_per_launch = args.stencil3d_depth
     w.setup()
     if args.temporal_depth > 0:  # after setup: overrides the autotuner's record
         A.set_temporal_depth(args.temporal_depth)
+        if args.tile_rows:
+            A.set_tile_rows(args.tile_rows)
     ev = Events(A)
     for _ in range(args.warmup):
         w.step()

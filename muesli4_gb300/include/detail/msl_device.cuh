@@ -256,13 +256,13 @@ MSL_DEV f32x2 pk2(float a, float b) {
     return d;
 }
 MSL_DEV float lo2(f32x2 v) {
-    float a, b;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    float a;
+    asm("{\n\t.reg .f32 t;\n\tmov.b64 {%0, t}, %1;\n\t}" : "=f"(a) : "l"(v));
     return a;
 }
 MSL_DEV float hi2(f32x2 v) {
-    float a, b;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    float b;
+    asm("{\n\t.reg .f32 t;\n\tmov.b64 {t, %0}, %1;\n\t}" : "=f"(b) : "l"(v));
     return b;
 }
 MSL_DEV f32x2 add2(f32x2 a, f32x2 b) {
