@@ -130,6 +130,38 @@ constexpr int kStageRows = 4, kStageCols = 4;
 template <typename S>
 MSL_DEV void stage_window(S *dst, const S *in, int pitch, int th, int nrows, int wx0, int wy0, int wz0, int depth,
                           int rows, int cols) {
+    // A single-plane window inside the grid whose rows start 16-byte aligned
+    // in global and shared memory: 16-byte copies without per-element tests,
+    // four loads in flight per thread. (dst is 16-byte aligned.)
+    constexpr int kV = 16 / (int)sizeof(S);
+    if (nrows == th && wz0 == 0 && depth == 1 && wx0 >= 0 && wy0 >= 0 && wx0 + pitch <= cols &&
+        wy0 + nrows <= rows && (wx0 % kV) == 0 && (pitch % kV) == 0 && (cols % kV) == 0 &&
+        ((uintptr_t)in % 16) == 0) {
+        const int vpr = pitch / kV, total = nrows * vpr;  // 16-byte vectors per row, in the window
+        const int q = (int)blockDim.x / vpr, rq = (int)blockDim.x - q * vpr;
+        int k = (int)threadIdx.x / vpr, v = (int)threadIdx.x - k * vpr;  // row and vector of item threadIdx.x
+        for (int i = threadIdx.x; i < total; i += 4 * (int)blockDim.x) {
+            uint4 val[4];
+            int kk[4], vv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                kk[u] = k;
+                vv[u] = v;
+                if (i + u * (int)blockDim.x < total)
+                    val[u] = *reinterpret_cast<const uint4 *>(in + (size_t)(wy0 + k) * cols + wx0 + v * kV);
+                k += q;  // next item: i + blockDim.x
+                v += rq;
+                if (v >= vpr) {
+                    v -= vpr;
+                    k++;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (i + u * (int)blockDim.x < total) reinterpret_cast<uint4 *>(dst + kk[u] * pitch)[vv[u]] = val[u];
+        }
+        return;
+    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     auto row_src = [&](int k, bool &row_in) {
         const int zz = k / th, gy = wy0 + (k - zz * th), gz = wz0 + zz;
@@ -264,9 +296,10 @@ constexpr int kPairRows = 4;
 // N) + S times 0.25, two cells per add.rn/mul.rn.f32x2; then cells on the
 // grid's edge -- and cells outside the grid, which are never stored -- keep
 // their value, as jacobi_strip_window computes them one by one. c returns the
-// cells' previous values.
+// cells' previous values. no_edge: the caller knows that no cell of the strip
+// lies on or beyond the grid's edge (the edge test is skipped).
 MSL_DEV void jacobi_pair_strip(const float *p, int pitch, int x, int y0, int cols, int rows,
-                               f32x2 (&c)[kPairRows], f32x2 (&v)[kPairRows]) {
+                               f32x2 (&c)[kPairRows], f32x2 (&v)[kPairRows], bool no_edge = false) {
     const f32x2 n = ld_pair(p - pitch), s = ld_pair(p + kPairRows * pitch);
 #pragma unroll
     for (int k = 0; k < kPairRows; k++) c[k] = ld_pair(p + k * pitch);
@@ -280,7 +313,7 @@ MSL_DEV void jacobi_pair_strip(const float *p, int pitch, int x, int y0, int col
         t = add2(t, k == kPairRows - 1 ? s : c[k + 1]);
         v[k] = mul2(t, pk2(0.25f, 0.25f));
     }
-    if (x >= 1 && x + 2 <= cols - 1 && y0 >= 1 && y0 + kPairRows <= rows - 1) return;  // no edge cell
+    if (no_edge || (x >= 1 && x + 2 <= cols - 1 && y0 >= 1 && y0 + kPairRows <= rows - 1)) return;  // no edge cell
     const bool xb0 = x <= 0 || x >= cols - 1, xb1 = x + 1 <= 0 || x + 1 >= cols - 1;
 #pragma unroll
     for (int k = 0; k < kPairRows; k++) {
@@ -424,11 +457,20 @@ MSL_DEV void tb_inner_sweeps(const Fn &fn, NPLMatrix<typename Compute<S>::type, 
             const int wc0 = x0 - wx0 - ext_e, wr0 = gy0 - wy0;
             const float *src = reinterpret_cast<const float *>(m.tile_);
             float *d = reinterpret_cast<float *>(dst);
+            // it / npairs as (it * inv) >> 20 with inv = ceil(2^20 / npairs):
+            // exact while it * (inv * npairs - 2^20) < 2^20; here npairs <=
+            // 64 (halo <= 31 at depth 32) and it < 2048 (64-row tiles), so the
+            // product stays below 2^17
+            const unsigned inv = ((1u << 20) + (unsigned)npairs - 1) / (unsigned)npairs;
+            // no strip cell within one cell of the grid's edge: the window
+            // (which holds every strip cell) lies inside the grid's interior
+            const bool no_edge =
+                wx0 >= 1 && wy0 >= 1 && wx0 + pitch <= cols - 1 && wy0 + BY + 2 * depth * r <= rows - 1;
             for (int it = threadIdx.x; it < ns * npairs; it += blockDim.x) {
-                const int sr = it / npairs, pc = it - sr * npairs;
+                const int sr = (int)(((unsigned)it * inv) >> 20), pc = it - sr * npairs;
                 const int wc = wc0 + 2 * pc, wr = wr0 + min(sr * kPairRows, H - kPairRows);
                 f32x2 c[kPairRows], v[kPairRows];
-                jacobi_pair_strip(src + wr * pitch + wc, pitch, wx0 + wc, wy0 + wr, cols, rows, c, v);
+                jacobi_pair_strip(src + wr * pitch + wc, pitch, wx0 + wc, wy0 + wr, cols, rows, c, v, no_edge);
 #pragma unroll
                 for (int k = 0; k < kPairRows; k++) st_pair(d + (wr + k) * pitch + wc, v[k]);
             }
