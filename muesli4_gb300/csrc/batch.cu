@@ -74,7 +74,14 @@ size_t resident_need(const Batch &b, int i) {
     return 2 * ((n * b.es + 127) / 128 * 128);
 }
 
-template <typename S> size_t round_smem(int depth) { return stencil2d_tb_smem<S>(1, depth); }
+template <typename S> size_t round_smem(int depth) {
+    return stencil2d_tb_smem<S>(1, depth, batch_tile_rows<S, JacobiSel>());
+}
+// Tile height of the batch's work-list: that of its plain rounds (defect
+// correction keeps 64 x 32 tiles for its defect kernel and correction rounds).
+int worklist_tile_rows(const Batch &b) {
+    return b.storage == MSL_F32 ? batch_tile_rows<float, JacobiSel>() : kSt2BY;
+}
 
 void destroy(Batch *b) {
     if (!b) return;
@@ -354,10 +361,11 @@ int msl_batch_create(int storage, int count, const int *rows, const int *cols, s
             b->worklist.push_back(i);
         }
     }
-    // Work-list tile prefix (64 x 32 tiles).
+    // Work-list tile prefix (64-column tiles of worklist_tile_rows rows).
+    const int ty = worklist_tile_rows(*b);
     for (int i : b->worklist) {
         b->host[i].first_tile = b->total_tiles;
-        b->total_tiles += (long long)((cols[i] + kSt2BX - 1) / kSt2BX) * ((rows[i] + kSt2BY - 1) / kSt2BY);
+        b->total_tiles += (long long)((cols[i] + kSt2BX - 1) / kSt2BX) * ((rows[i] + ty - 1) / ty);
     }
     std::vector<int> lists(b->resident);
     lists.insert(lists.end(), b->worklist.begin(), b->worklist.end());
@@ -366,7 +374,7 @@ int msl_batch_create(int storage, int count, const int *rows, const int *cols, s
         std::vector<int> tg((size_t)b->total_tiles);
         for (size_t w = 0; w < b->worklist.size(); w++) {
             const BatchGrid &gd = b->host[b->worklist[w]];
-            const long long nt = (long long)((gd.cols + kSt2BX - 1) / kSt2BX) * ((gd.rows + kSt2BY - 1) / kSt2BY);
+            const long long nt = (long long)((gd.cols + kSt2BX - 1) / kSt2BX) * ((gd.rows + ty - 1) / ty);
             for (long long t = 0; t < nt; t++) tg[(size_t)(gd.first_tile + t)] = (int)w;
         }
         e = cudaMalloc(&b->d_tile_grid, tg.size() * sizeof(int));

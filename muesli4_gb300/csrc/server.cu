@@ -218,7 +218,8 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
             }
             BatchGrid g = grid2d(r);
             g.first_tile = tiles;
-            const long long nt = (long long)((r->cols + kSt2BX - 1) / kSt2BX) * ((r->rows + kSt2BY - 1) / kSt2BY);
+            constexpr int ty = batch_tile_rows<float, JacobiSel>();  // the work-list round's tile height
+            const long long nt = (long long)((r->cols + kSt2BX - 1) / kSt2BX) * ((r->rows + ty - 1) / ty);
             tiles += nt;
             s.map2.insert(s.map2.end(), (size_t)nt, (int)s.h2.size());
             s.h2.push_back(g);
@@ -274,7 +275,7 @@ cudaError_t run_interval(Server &s, const std::vector<Request *> &act) {
         if (tiles) {
             SERVE_TRY(upload_map(s.map2, &s.d_map2, &s.cap_map2, s.s2));
             const int depth = s.depth2d;
-            const size_t smem = stencil2d_tb_smem<float>(1, depth);
+            const size_t smem = stencil2d_tb_smem<float>(1, depth, batch_tile_rows<float, JacobiSel>());
             auto rk = batch_round_kernel<float>;
             if (smem > 48 * 1024)
                 SERVE_TRY(cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -245,6 +245,13 @@ __global__ void __launch_bounds__(kBatchResidentThreads)
     }
 }
 
+// Tile height of the work-list rounds: FP32 Jacobi rounds (packed-pair
+// strips) take 64 x 64 tiles -- less halo recomputed per useful update, and
+// the strips of a sweep fill the CTA's passes better -- the others 64 x 32.
+template <typename S, class Sel> constexpr int batch_tile_rows() {
+    return std::is_same<S, float>::value && std::is_same<Sel, JacobiSel>::value ? 64 : kSt2BY;
+}
+
 // One round of the work-list grids: every tile of every unfinished grid does
 // `depth` sweeps from buf[cur] to buf[cur ^ 1] (each grid's own direction, so
 // grids that joined at different times can share a round). Plain coalesced loads
@@ -255,10 +262,11 @@ __global__ void __launch_bounds__(kSt2Threads)
     batch_round_kernel(BatchGrid *grids, const int *list, const int *tile_grid, long long total_tiles, int depth,
                        int check, unsigned *ticket, int nlist, double tol, long long max_iters, int *active) {
     using T = typename Compute<S>::type;
+    constexpr int BY = batch_tile_rows<S, Sel>();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int r = 1;
     const int hx = halo_x<S>(depth * r);
-    const int pitch = kSt2BX + 2 * hx, th = kSt2BY + 2 * depth * r;
+    const int pitch = kSt2BX + 2 * hx, th = BY + 2 * depth * r;
     const int buf_elems = (pitch * th * (int)sizeof(S) + 127) / 128 * 128 / (int)sizeof(S);
     S *buf0 = reinterpret_cast<S *>(smem_raw + kStHeader);
     S *buf1 = buf0 + buf_elems;
@@ -270,7 +278,7 @@ __global__ void __launch_bounds__(kSt2Threads)
         const int rows = g.rows, cols = g.cols;
         const int tiles_x = (cols + kSt2BX - 1) / kSt2BX;
         const unsigned t = (unsigned)(item - g.first_tile);  // < 2^30 cells / 2048 per tile
-        const int x0 = (int)(t % (unsigned)tiles_x) * kSt2BX, y0 = (int)(t / (unsigned)tiles_x) * kSt2BY;
+        const int x0 = (int)(t % (unsigned)tiles_x) * kSt2BX, y0 = (int)(t / (unsigned)tiles_x) * BY;
         const S *in = (const S *)g.buf[g.cur];
         S *out = (S *)g.buf[g.cur ^ 1];
         const int wx0 = x0 - hx, wy0 = y0 - depth * r;
@@ -288,14 +296,14 @@ __global__ void __launch_bounds__(kSt2Threads)
         m.oy_ = wy0;
         m.pitch_ = pitch;
         m.tile_h_ = th;
-        tb_inner_sweeps<S>(fn, m, buf0, buf1, x0, y0, rows, cols, r, depth, pitch, wx0, wy0);
+        tb_inner_sweeps<S, BY>(fn, m, buf0, buf1, x0, y0, rows, cols, r, depth, pitch, wx0, wy0);
         const int x = x0 + (warp % (kSt2BX / 32)) * 32 + lane;
         const int ys = y0 + (warp / (kSt2BX / 32)) * kSt2RPT;
         double dmax = 0.0;
         if constexpr (has_pair_strip<std::remove_cv_t<decltype(fn)>>::value && std::is_same<S, float>::value) {
             jacobi_pair_block(reinterpret_cast<const float *>(m.tile_), pitch, wx0, wy0, x0, y0, rows, cols,
-                              reinterpret_cast<float *>(out), check != 0, dmax);
-        } else if (x0 - r >= 0 && y0 - r >= 0 && x0 + kSt2BX + r <= cols && y0 + kSt2BY + r <= rows) {
+                              reinterpret_cast<float *>(out), check != 0, dmax, BY);
+        } else if (x0 - r >= 0 && y0 - r >= 0 && x0 + kSt2BX + r <= cols && y0 + BY + r <= rows) {
             m.check_ = false;
             stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, check != 0, dmax);
         } else {

@@ -15,9 +15,9 @@
 // inputs, which the caller guarantees (this kernel is used only on the
 // outputs of Life sweeps).
 //
-// One CTA computes a 960 x 64 block `depth` generations ahead (depth <= 32).
+// One CTA computes a 960 x 128 block `depth` generations ahead (depth <= 32).
 // Its window is 32 words (1024 cells) wide -- one word per lane, one word of
-// halo either side -- and 64 + 2 depth rows high. Staging: each warp reads
+// halo either side -- and 128 + 2 depth rows high. Staging: each warp reads
 // whole window rows with coalesced 4-byte loads (zeros outside the grid) and
 // packs 32 cells into a word with one ballot. Generations ping-pong between
 // two bit buffers; a warp computes a strip of 8 rows for all 32 words of the
@@ -42,7 +42,7 @@ constexpr int kLifeWords = 32;                  // words per window row, one per
 constexpr int kLifePitch = kLifeWords + 2;      // plus a zero pad either side
 constexpr int kLifeBW = kLifeWords - 2;         // words per block row
 constexpr int kLifeBX = kLifeBW * 32;           // 960 cells
-constexpr int kLifeBY = 64;                     // block rows
+constexpr int kLifeBY = 128;                    // block rows (taller blocks recompute less halo per generation)
 constexpr int kLifeWarps = 8, kLifeThreads = 32 * kLifeWarps;
 constexpr int kLifeStrip = 8;                   // rows per warp task (vertical reuse of the row sums)
 constexpr int kLifeMaxDepth = 32;               // generations per launch (the block's column halo)
@@ -116,7 +116,7 @@ MSL_DEV uint32_t life_colmask(int gx0, int cols) {
     return hi - lo == 32 ? 0xFFFFFFFFu : ((1u << (hi - lo)) - 1u) << lo;
 }
 
-static __global__ void __launch_bounds__(kLifeThreads, 8)
+static __global__ void __launch_bounds__(kLifeThreads, 4)
     life_bits_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, int rows, int cols, int depth) {
     extern __shared__ uint32_t life_smem[];
     const int th = kLifeBY + 2 * depth;  // window rows
@@ -185,7 +185,8 @@ inline cudaError_t launch_life_packed(const int32_t *in, int32_t *out, int rows,
                                       cudaStream_t st) {
     const int gy = (rows + kLifeBY - 1) / kLifeBY;
     if (depth < 1 || depth > kLifeMaxDepth || in == out || gy > 65535) return cudaErrorNotSupported;
-    const size_t smem = life_bits_smem(depth);  // <= 34816 bytes
+    const size_t smem = life_bits_smem(depth);  // <= 52224 bytes
+    if (smem > 48 * 1024) cudaFuncSetAttribute(life_bits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid((cols + kLifeBX - 1) / kLifeBX, gy);
     life_bits_kernel<<<grid, kLifeThreads, smem, st>>>(in, out, rows, cols, depth);
     return cudaGetLastError();

@@ -323,35 +323,38 @@ MSL_DEV void jacobi_pair_strip(const float *p, int pitch, int x, int y0, int col
     }
 }
 
-// The sweep of a 64 x (kPairRows * warps) block to global memory on packed
-// pairs: thread t owns columns x0 + 2 (t % 32) and the next, rows y0 +
-// kPairRows (t / 32) onwards. win: the window holding the sweep's input
-// (origin wx0, wy0). With want, the FP64 max |new - old| of the stored cells
-// into dmax.
+// The sweep of a 64 x by block to global memory on packed pairs: lane l of
+// warp w owns columns x0 + 2 l and the next of the strips of rows y0 +
+// kPairRows (w + k nwarps). win: the window holding the sweep's input (origin
+// wx0, wy0). With want, the FP64 max |new - old| of the stored cells into
+// dmax.
 MSL_DEV void jacobi_pair_block(const float *win, int pitch, int wx0, int wy0, int x0, int y0, int rows, int cols,
-                               float *out, bool want, double &dmax) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int x = x0 + 2 * lane, y = y0 + kPairRows * warp;
-    f32x2 c[kPairRows], v[kPairRows];
-    jacobi_pair_strip(win + (y - wy0) * pitch + (x - wx0), pitch, x, y, cols, rows, c, v);
+                               float *out, bool want, double &dmax, int by) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int x = x0 + 2 * lane;
     const bool pairs = (cols & 1) == 0 && ((uintptr_t)out & 7) == 0 && x + 1 < cols;
+    for (int sidx = warp; sidx < by / kPairRows; sidx += nwarps) {
+        const int y = y0 + kPairRows * sidx;
+        f32x2 c[kPairRows], v[kPairRows];
+        jacobi_pair_strip(win + (y - wy0) * pitch + (x - wx0), pitch, x, y, cols, rows, c, v);
 #pragma unroll
-    for (int k = 0; k < kPairRows; k++) {
-        if (y + k >= rows || x >= cols) break;
-        float *o = out + (size_t)(y + k) * cols + x;
-        if (want) {
-            const double d0 = fabs((double)lo2(v[k]) - (double)lo2(c[k]));
-            if (d0 > dmax || d0 != d0) dmax = d0;
-            if (x + 1 < cols) {
-                const double d1 = fabs((double)hi2(v[k]) - (double)hi2(c[k]));
-                if (d1 > dmax || d1 != d1) dmax = d1;
+        for (int k = 0; k < kPairRows; k++) {
+            if (y + k >= rows || x >= cols) break;
+            float *o = out + (size_t)(y + k) * cols + x;
+            if (want) {
+                const double d0 = fabs((double)lo2(v[k]) - (double)lo2(c[k]));
+                if (d0 > dmax || d0 != d0) dmax = d0;
+                if (x + 1 < cols) {
+                    const double d1 = fabs((double)hi2(v[k]) - (double)hi2(c[k]));
+                    if (d1 > dmax || d1 != d1) dmax = d1;
+                }
             }
-        }
-        if (pairs) {
-            st_pair(o, v[k]);
-        } else {
-            o[0] = lo2(v[k]);
-            if (x + 1 < cols) o[1] = hi2(v[k]);
+            if (pairs) {
+                st_pair(o, v[k]);
+            } else {
+                o[0] = lo2(v[k]);
+                if (x + 1 < cols) o[1] = hi2(v[k]);
+            }
         }
     }
 }
@@ -566,7 +569,7 @@ __global__ void __launch_bounds__(kSt2Threads)
     if constexpr (has_pair_strip<Fn>::value && std::is_same<S, float>::value) {
         static_assert(kSt2Threads == 32 * (kSt2BY / kPairRows), "one pair strip per thread");
         jacobi_pair_block(reinterpret_cast<const float *>(tile), pitch, wx0, wy0, x0, y0, rows, cols,
-                          reinterpret_cast<float *>(out), want, dmax);
+                          reinterpret_cast<float *>(out), want, dmax, kSt2BY);
     } else if (interior) {
         m.check_ = false;
         stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, want, dmax);
@@ -641,7 +644,7 @@ __global__ void __launch_bounds__(BY * 8)
     if constexpr (has_pair_strip<Fn>::value && std::is_same<S, float>::value) {
         static_assert(BY * 8 == 32 * (BY / kPairRows), "one pair strip per thread");
         jacobi_pair_block(reinterpret_cast<const float *>(m.tile_), pitch, wx0, wy0, x0, y0, rows, cols,
-                          reinterpret_cast<float *>(out), want, dmax);
+                          reinterpret_cast<float *>(out), want, dmax, BY);
     } else if (interior) {
         m.check_ = false;
         stencil2d_strip<S, true>(fn, m, x, ys, rows, cols, out, want, dmax);
