@@ -293,7 +293,10 @@ constexpr int kPairRows = 4;
 // Plain Jacobi for the cells (x, y0 + k) and (x + 1, y0 + k), k < kPairRows,
 // read from the window only (p: the window address of (x, y0), 8-byte
 // aligned; rows pitch apart): heat2D of the four neighbours, (((0 + W) + E) +
-// N) + S times 0.25, two cells per add.rn/mul.rn.f32x2; then cells on the
+// N) + S times 0.25, two cells per add.rn/fma.rn.f32x2, computed as
+// fma(((W + E) + N) + S, 0.25, +0): the sums differ only when all four terms
+// are -0 (-0 against +0), and adding +0 after the exact product turns that -0
+// into +0 without changing any other result; then cells on the
 // grid's edge -- and cells outside the grid, which are never stored -- keep
 // their value, as jacobi_strip_window computes them one by one. c returns the
 // cells' previous values. no_edge: the caller knows that no cell of the strip
@@ -307,11 +310,10 @@ MSL_DEV void jacobi_pair_strip(const float *p, int pitch, int x, int y0, int col
     for (int k = 0; k < kPairRows; k++) {
         const f32x2 w = pk2(p[k * pitch - 1], lo2(c[k]));
         const f32x2 e = pk2(hi2(c[k]), p[k * pitch + 2]);
-        f32x2 t = add2(pk2(0.0f, 0.0f), w);
-        t = add2(t, e);
+        f32x2 t = add2(w, e);
         t = add2(t, k == 0 ? n : c[k - 1]);
         t = add2(t, k == kPairRows - 1 ? s : c[k + 1]);
-        v[k] = mul2(t, pk2(0.25f, 0.25f));
+        v[k] = fma2(t, pk2(0.25f, 0.25f), pk2(0.0f, 0.0f));
     }
     if (no_edge || (x >= 1 && x + 2 <= cols - 1 && y0 >= 1 && y0 + kPairRows <= rows - 1)) return;  // no edge cell
     const bool xb0 = x <= 0 || x >= cols - 1, xb1 = x + 1 <= 0 || x + 1 >= cols - 1;

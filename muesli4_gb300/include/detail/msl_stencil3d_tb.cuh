@@ -64,10 +64,14 @@ inline size_t stencil3d_ztb_smem() {
 template <class Fn, class = void> struct IsSum7Div6 : std::false_type {};
 template <class Fn> struct IsSum7Div6<Fn, std::void_t<decltype(Fn::kSum7Div6)>> : std::bool_constant<Fn::kSum7Div6> {};
 
-// heat3D's sum of six neighbours in its order, (((((0 + w) + e) + n) + s) + b) + f, for a pair.
+// heat3D's sum of six neighbours for a pair, without the order's leading
+// 0 + w: ((((w + e) + n) + s) + b) + f. It equals (((((0 + w) + e) + n) + s) +
+// b) + f except when every term is -0 (then -0 against +0: the chain from +0
+// never reaches -0, and once a nonzero term or a +0 enters, both chains agree
+// from there on). Such a sum lies outside the division's fast-path range, and
+// div6_pairs' fallback adds +0 before dividing, so the quotient is the same.
 MSL_DEV f32x2 sum7x2(f32x2 w, f32x2 e, f32x2 n, f32x2 s, f32x2 b, f32x2 f) {
-    f32x2 v = add2(pk2(0.0f, 0.0f), w);
-    v = add2(v, e);
+    f32x2 v = add2(w, e);
     v = add2(v, n);
     v = add2(v, s);
     v = add2(v, b);
@@ -103,8 +107,9 @@ MSL_DEV bool strip_in_range(const f32x2 (&v)[4]) {
     return r != 0;
 }
 // IEEE-correct x / 6 for sums outside the fast path's range; out of line so
-// that the rare path does not crowd the march's instruction cache.
-static __device__ __noinline__ float div6_cold(float x) { return div6_rn(x); }
+// that the rare path does not crowd the march's instruction cache. The +0
+// turns a -0 sum of sum7x2 into the +0 that the reference's order yields.
+static __device__ __noinline__ float div6_cold(float x) { return div6_rn(__fadd_rn(x, 0.0f)); }
 
 // x / 6 for the four pairs of a strip: the fast path for the whole warp when
 // every lane's `good` holds (its live cells' sums lie in the fast path's

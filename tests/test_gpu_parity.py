@@ -383,6 +383,32 @@ def test_stencil3d_heat_z_marching(gpu, shape, sweeps_per_launch):
         gpu.set_stencil3d_depth(2)
 
 
+@pytest.mark.parametrize("depth", [1, 2, 4, 8])
+def test_jacobi_negative_zero_block(gpu, depth):
+    """A block of -0 cells: a cell whose four neighbours are all -0 sums to +0
+    in the reference's order (((0 + W) + E) + N) + S, and its value stays +0
+    after the multiplication by 0.25 -- on the one-sweep, temporal-blocking and
+    batch paths alike, against the oracle."""
+    g = W.jacobi_grid(200, 300, 21)  # too large for a CTA-resident solve: the batch's work-list rounds
+    g[40:160, 60:240] = np.float32(-0.0)
+    gpu.set_temporal_depth(depth)
+    try:
+        a, b = dev(gpu, g), gpu.DeviceArray(g.shape, g.dtype)
+        last, res = gpu.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, a, b, 1, 0.0, 8)
+    finally:
+        gpu.set_temporal_depth(0)
+    want, _, want_res = O.stencil2d_iterate(gpu.MSL_ST2_JACOBI5, g, 1, 0.0, 8)
+    assert bits_equal(last.download(), want)
+    assert res == want_res
+    batch = gpu.Batch([g.shape])
+    try:
+        batch.set_grid(0, g)
+        batch.solve(tol=0.0, max_iters=8, check_every=8, depth=depth)
+        assert bits_equal(batch.get_grid(0)[0], want)
+    finally:
+        batch.close()
+
+
 @pytest.mark.parametrize("zchunk", [1, 2, 3, 7, 24, 0])
 def test_stencil3d_heat_z_chunks(gpu, zchunk):
     """The z-marching kernel's result does not depend on how the depth is cut
@@ -414,6 +440,7 @@ def test_stencil3d_heat_special_values(gpu, sweeps_per_launch):
     x[(u >= 0.02) & (u < 0.025)] = np.float32(np.inf)
     x[(u >= 0.025) & (u < 0.05)] *= np.float32(-0.3)
     x[8:16, 16:24, 24:32] = 0.0
+    x[20:28, 30:38, 40:48] = np.float32(-0.0)  # all six neighbours -0: the sum is +0 in the reference's order
     gpu.set_stencil3d_depth(sweeps_per_launch)
     try:
         for iters in (1, 2, 4):
