@@ -1046,8 +1046,11 @@ def main():
     dist.barrier()
     t0 = time.perf_counter()
     e_a = ev.record()
+    e2e_steps_ms = []
     for _ in range(args.steps):
+        t_s = time.perf_counter()
         w.e2e_step()
+        e2e_steps_ms.append((time.perf_counter() - t_s) * 1e3)
     e_b = ev.record()
     A.sync()
     e2e_s = max(time.perf_counter() - t0, ev.ms(e_a, e_b) / 1e3)
@@ -1096,7 +1099,10 @@ def main():
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": w.dtype, "data": "synthetic",
             "config": dict(w.config(), parallelism=f"replicas x{dist.world}", **getattr(w, "tuned", {})),
-            "e2e": {"value": e2e_value, "unit": w.unit, "h2d_bytes_per_step": w.h2d, "d2h_bytes_per_step": w.d2h},
+            "e2e": {"value": e2e_value, "unit": w.unit, "h2d_bytes_per_step": w.h2d, "d2h_bytes_per_step": w.d2h,
+                    # host-clock time of each end-to-end step: single slow steps (the host link is
+                    # shared) move the whole-run value, which is total updates over total time
+                    "step_ms_median": statistics.median(e2e_steps_ms), "step_ms_max": max(e2e_steps_ms)},
             "roofline": {"bound": "hbm", "kernel": p.name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "bytes_per_launch": p.bytes_per_launch,

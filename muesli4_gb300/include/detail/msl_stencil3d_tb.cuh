@@ -341,13 +341,13 @@ __global__ void __launch_bounds__(kZtbThreads, kZtbMinCtas)
     }
 }
 
-// z planes per CTA: the longest chunk (24 planes down to 4) that still gives
+// z planes per CTA: the longest chunk (26 planes down to 4) that still gives
 // at least two waves of resident CTAs. Longer chunks spend less on the first
 // sweep's two extra planes and the march's start; on heat3D 512^3 (128 tiles,
-// 456 resident CTAs) 24 planes measured best (11.7 ms per 100 sweeps against
-// 12.0 for 16 and 11.8 for 32).
+// 456 resident CTAs) 26 planes measured best (10.67 ms per 100 sweeps against
+// 10.79 for 24, 10.89 for 20 and 22, 10.97 for 28, 11.1 for 32).
 inline int stencil3d_ztb_zchunk(int depth, long long tiles, long long resident) {
-    static const int kCand[] = {24, 16, 12, 8, 6, 4};
+    static const int kCand[] = {26, 24, 16, 12, 8, 6, 4};
     for (int z : kCand)
         if (tiles * ((depth + z - 1) / z) >= 2 * resident) return z;
     return 4;
