@@ -28,7 +28,7 @@ struct Sweep {
 std::atomic<int> g_persistent3d{-1};
 // Sweeps per launch of msl_stencil3d_iterate where the z-marching kernel
 // applies (1 or 2). Two is the default: on heat3D 512^3 the two-sweep kernel
-// (half the HBM traffic per sweep, bound by instruction issue) runs 1.4x the
+// (half the HBM traffic per sweep, bound by instruction issue) runs 1.5x the
 // one-sweep kernel, which is itself at the HBM roofline.
 std::atomic<int> g_depth3d{2};
 // z planes per CTA of the z-marching kernel (0: chosen per grid).
