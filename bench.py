@@ -409,7 +409,7 @@ class Jacobi:
         d = getattr(self, "fixed_depth", 0)
         rows = getattr(self, "fixed_tile_rows", 0) or 32
         if d <= 0:
-            d, rows, _ = A.autotune_stencil2d_shape(A.MSL_ST2_JACOBI5, A.MSL_F32, self.side, self.side, 1, 64)
+            d, rows, _ = A.autotune_stencil2d_shape(A.MSL_ST2_JACOBI5, A.MSL_F32, self.side, self.side, 1, self.iters)
         tiles = ((self.side + 63) // 64) * ((self.side + rows - 1) // rows)
         self.tuned = {"temporal_depth": d, "tile": f"64x{rows}" if d > 1 else "64x32 (one sweep per launch)",
                       "threads_per_cta": rows * 8 if d > 1 else 256, "ctas": tiles}

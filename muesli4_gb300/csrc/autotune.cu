@@ -114,10 +114,11 @@ int msl_autotune_stencil2d_shape(int dtype, int kind, int rows, int cols, int ra
             if (tiles_vary || t == 32) candidates[ncand++] = Cand{d, t};
     double rate[1 + 9 * 3] = {};
     bool usable[1 + 9 * 3] = {};
-    // Warm every shape up once, then time each three times, interleaved, and
+    // Warm every shape up once, then time each five times, interleaved, and
     // keep each shape's best run (clock ramps and other work on the GPU slow
-    // single runs down, never speed them up).
-    for (int round = 0; round < 4 && rc == MSL_OK; round++) {
+    // single runs down, never speed them up; shapes within a few per cent of
+    // each other swap places between single runs).
+    for (int round = 0; round < 6 && rc == MSL_OK; round++) {
         for (int k = 0; k < ncand; k++) {
             const int d = candidates[k].depth;
             if (d > iters || (round > 0 && !usable[k])) continue;
