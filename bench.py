@@ -27,6 +27,7 @@ reference's OpenMP loops) timed on a bounded sample on this host's cores.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -1011,6 +1012,10 @@ def main():
     A.sync()
 
     # ---- device-resident timed region ----
+    # (the host's garbage collector stays off inside both timed regions: a
+    # collection pass would be host noise, not the library's time)
+    gc.collect()
+    gc.disable()
     dist.barrier()
     A.sync()
     sampler = ClockSampler(dist.local_rank)
@@ -1054,6 +1059,7 @@ def main():
     e_b = ev.record()
     A.sync()
     e2e_s = max(time.perf_counter() - t0, ev.ms(e_a, e_b) / 1e3)
+    gc.enable()
     e2e_s = dist.max(e2e_s)
     e2e_value = dist.sum(w.updates() * args.steps) / e2e_s / 1e9
     # the pipelined downloads must have read the finished results
