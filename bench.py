@@ -260,7 +260,7 @@ class StencilSuite:
             # compulsory bytes one read and one write of the cube
             k = max(1, getattr(self, "heat_sweeps_per_launch", 1))
             p = self.parts["heat"]
-            p.launches = self.heat_steps // k + self.heat_steps % k
+            p.launches = heat_launches(self.heat_steps, k)
             p.bytes_per_launch = 8 * m ** 3 * self.heat_steps // p.launches
             p.sweeps_per_launch = k
             self.tuned["heat_sweeps_per_launch"] = k
@@ -933,6 +933,13 @@ def run_batch(args, dist: Dist):
             "gpu_launches": launches, "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
+
+
+def heat_launches(steps, sweeps_per_launch):
+    """Launches of a heat3D iteration: `sweeps_per_launch` sweeps per launch
+    (the z-marching kernel's two), an odd last sweep on its own."""
+    k = max(1, sweeps_per_launch)
+    return steps // k + steps % k
 
 
 def life_launches(steps, depth):

@@ -1,6 +1,6 @@
 """bench.py's JSON contract where it runs without a GPU: the reference arm
 (the CPU implementation of the path, timed on a bounded sample) and the
-launch bookkeeping of the Life part."""
+launch bookkeeping of the Life and heat3D parts."""
 import json
 import os
 import subprocess
@@ -20,6 +20,14 @@ def test_life_launch_count():
     assert bench.life_launches(200, 1) == 200
     assert bench.life_launches(200, 8) == 26
     assert bench.life_launches(1, 32) == 1
+
+
+def test_heat_launch_count():
+    # two sweeps per launch on the z-marching kernel, an odd last sweep alone
+    assert bench.heat_launches(100, 2) == 50
+    assert bench.heat_launches(101, 2) == 51
+    assert bench.heat_launches(100, 1) == 100
+    assert bench.heat_launches(1, 2) == 1
 
 
 @pytest.mark.timeout(300)
