@@ -174,6 +174,8 @@ __global__ void __launch_bounds__(kZtbThreads, kZtbMinCtas)
     const int mo = my * P + mx, mo_mid = mo - P;
     const bool m_in = wx0 + mx >= 0 && wx0 + mx < cols && wy0 + my >= 0 && wy0 + my < rows;
 
+    __shared__ int s_fail;  // set by the leader when a plane's wait gives up
+    if (threadIdx.x == 0) s_fail = 0;
     uint32_t phase = 0, pending = 0;  // leader: per slot, the parity of its next completion / a load not waited for
     auto slot = [&](int p) { return in_ring + (p & 3) * kZtbPlane; };
     auto issue = [&](int p) {  // leader: TMA load of input plane p (zeros outside the grid)
@@ -314,9 +316,9 @@ __global__ void __launch_bounds__(kZtbThreads, kZtbMinCtas)
                 }
             }
         }
-        bool good = true;
-        if (leader && t + 3 <= ze + 1) good = wait_plane(t + 3);  // read from step t+1 on
-        return __syncthreads_and(good);
+        if (leader && t + 3 <= ze + 1 && !wait_plane(t + 3)) s_fail = 1;  // read from step t+1 on
+        __syncthreads();
+        return s_fail == 0;
     };
     auto march = [&](auto full_tag, auto want_tag) {
         for (int t = zb - 2; ok && t < ze; t += 3) {
