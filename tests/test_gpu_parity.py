@@ -440,6 +440,12 @@ def test_stencil3d_heat_special_values(gpu, sweeps_per_launch):
     x[(u >= 0.02) & (u < 0.025)] = np.float32(np.inf)
     x[(u >= 0.025) & (u < 0.05)] *= np.float32(-0.3)
     x[8:16, 16:24, 24:32] = 0.0
+    # isolated cells in the zero block: a neighbour's sum is the cell alone,
+    # just below, at and above the fast division's lower bound 2^-122, and
+    # between it and 2^-121 (quotients near 2^-124)
+    t = np.float32(2.0 ** -122)
+    for k, f in enumerate((1.0, 1.25, 1.4999999, 1.5, 1.5000001, 2.0, 0.999999)):
+        x[9 + (k % 3) * 2, 17 + k, 25 + (k % 2) * 3] = np.float32(f) * t * np.float32(1 if k % 2 else -1)
     x[20:28, 30:38, 40:48] = np.float32(-0.0)  # all six neighbours -0: the sum is +0 in the reference's order
     gpu.set_stencil3d_depth(sweeps_per_launch)
     try:
