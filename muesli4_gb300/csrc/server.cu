@@ -28,6 +28,7 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -849,12 +850,13 @@ int msl_server_restore(const char *path, void **server) {
         ok = fread(recs.data(), sizeof(CkptRecord), recs.size(), f) == recs.size();
     }
     std::vector<std::unique_ptr<Request>> reqs;
+    std::set<long long> ids;  // a request id appears once: the server's table is keyed by it
     for (size_t i = 0; ok && i < recs.size(); i++) {
         const CkptRecord &c = recs[i];
         ok = (c.kind == MSL_SERVE_JACOBI2D || c.kind == MSL_SERVE_HEAT3D) &&
              (c.state == kQueued || c.state == kRunning || c.state == kDone) && c.depth >= 1 && c.rows >= 1 &&
              c.cols >= 1 && (long long)c.depth * c.rows * c.cols <= (1LL << 31) - 1 && c.iters >= 0 &&
-             c.iters % h.check_every == 0 && c.id > 0 && c.id < h.next_id;
+             c.iters % h.check_every == 0 && c.id > 0 && c.id < h.next_id && ids.insert(c.id).second;
         if (!ok) break;
         auto r = std::make_unique<Request>();
         r->id = c.id;

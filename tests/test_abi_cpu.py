@@ -102,3 +102,33 @@ def test_tile_rows_setter_needs_no_device(lib):
     assert lib.msl_set_tile_rows(24) == bad and lib.msl_set_tile_rows(-1) == bad and lib.msl_set_tile_rows(128) == bad
     for ok in (16, 32, 64, 0):
         assert lib.msl_set_tile_rows(ok) == abi.MSL_OK
+
+
+def _server_checkpoint(records):
+    """A server checkpoint in the library's layout: magic, header (tol,
+    max_iters, check_every, depth2d, budget, next_id, count), one record per
+    request (id, kind, state, depth, rows, cols, pad, iters, residual), then
+    every request's FP32 cells in record order."""
+    import struct
+    out = b"MSLSRV01" + struct.pack("<dqiiQqq", 1e-4, 1000, 10, 2, 0, 10, len(records))
+    for rid, state in records:
+        out += struct.pack("<qiiiiiiqd", rid, 0, state, 1, 3, 4, 0, 20, 0.5)
+    for _ in records:
+        out += struct.pack("<12f", *range(12))
+    return out
+
+
+def test_server_restore_rejects_repeated_request_ids(lib, tmp_path):
+    """The restore parses and checks the whole file before it touches the
+    device: a well-formed checkpoint gets as far as starting a server (which
+    needs msl_init), one that names a request id twice is rejected."""
+    import ctypes
+    h = ctypes.c_void_p()
+    good = tmp_path / "good.ckpt"
+    good.write_bytes(_server_checkpoint([(1, 0), (2, 1), (3, 2)]))
+    assert lib.msl_server_restore(str(good).encode(), ctypes.byref(h)) == abi.MSL_ERR_NOT_INITIALIZED
+    bad = tmp_path / "repeated.ckpt"
+    bad.write_bytes(_server_checkpoint([(1, 0), (2, 1), (1, 1)]))
+    assert lib.msl_server_restore(str(bad).encode(), ctypes.byref(h)) == abi.MSL_ERR_INVALID_ARGUMENT
+    assert b"not a complete server checkpoint" in lib.msl_last_error_string()
+    assert not h.value
