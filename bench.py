@@ -950,8 +950,8 @@ def life_launches(steps, depth):
 
 DRAM_TRAFFIC_PER_LAUNCH = {
     "heat3d": 1090.23e6,         # profiles/heat7_zmarch_512.md (two sweeps of 512^3 per launch)
-    "heat3d/1": 1027.49e6,       # profiles/heat7_stencil3d_512.md (one sweep of 512^3)
-    "life": 480.17e6,            # profiles/life_bits_stencil2d_8192.md (32 generations of 8192^2)
+    "heat3d/1": 1026.96e6,       # profiles/heat7_stencil3d_512.md (one sweep of 512^3)
+    "life": 479.4e6,             # profiles/life_bits_stencil2d_8192.md (32 generations of 8192^2)
     "box_mean_r1-10": 495.08e6,  # profiles/boxmean_r10_box2d_pair_8192.md (r = 10)
 }
 
