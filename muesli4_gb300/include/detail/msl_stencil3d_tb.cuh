@@ -127,7 +127,10 @@ MSL_DEV void div6_pairs(bool good, f32x2 (&x)[4]) {
 // Three CTAs per SM (80 registers, 61 KB each): measured faster than two
 // CTAs with the registers the march would take unbounded (114).
 constexpr int kZtbMinCtas = 3;
-template <class Fn>
+// kResid: the launch folds max |new - old| of the second sweep into *resid
+// (one instantiation each, so that registers are allocated for the form that
+// runs).
+template <class Fn, bool kResid>
 __global__ void __launch_bounds__(kZtbThreads, kZtbMinCtas)
     stencil3d_ztb_kernel(const __grid_constant__ CUtensorMap tmap, float *out, int depth, int rows, int cols,
                          int zchunk, Fn fn, unsigned long long *resid, unsigned *err) {
@@ -234,7 +237,6 @@ __global__ void __launch_bounds__(kZtbThreads, kZtbMinCtas)
     }
     __syncthreads();  // plane zb-2's slot is read before step zb-2 reloads it
 
-    const bool want = resid != nullptr;
     double dmax = 0.0;
     auto live_row = [&](auto full_tag, int j) {
         constexpr bool FULL = decltype(full_tag)::value;
@@ -327,17 +329,12 @@ __global__ void __launch_bounds__(kZtbThreads, kZtbMinCtas)
             if (ok && t + 2 < ze) ok = step(full_tag, want_tag, t + 2, ic, ia, ib, mc, ma, mb, pc, pb);
         }
     };
-    // one march per case, so that the common one (every strip cell inside,
-    // no residual) carries no tests it does not need
-    if (full) {
-        if (want) march(std::true_type{}, std::true_type{});
-        else march(std::true_type{}, std::false_type{});
-    } else {
-        if (want) march(std::false_type{}, std::true_type{});
-        else march(std::false_type{}, std::false_type{});
-    }
+    // one march per case, so that the common one (every strip cell inside)
+    // carries no tests it does not need
+    if (full) march(std::true_type{}, std::bool_constant<kResid>{});
+    else march(std::false_type{}, std::bool_constant<kResid>{});
     if (!ok && leader) drain();
-    if (want) {
+    if constexpr (kResid) {
         dmax = block_max(dmax);
         if (threadIdx.x == 0) atomic_max_nonneg(resid, dmax);
     }
@@ -373,9 +370,9 @@ cudaError_t launch_stencil3d_ztb(const float *in, float *out, int depth, int row
                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorNotSupported;
     const size_t smem = stencil3d_ztb_smem();
-    auto k = stencil3d_ztb_kernel<Fn>;
+    auto k = resid ? stencil3d_ztb_kernel<Fn, true> : stencil3d_ztb_kernel<Fn, false>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    static int per_sm = 0, sms = 0;  // per instantiation
+    static int per_sm = 0, sms = 0;  // per functor; both forms share launch bounds and shared memory
     if (per_sm == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
