@@ -414,7 +414,8 @@ int msl_server_stop(void *server);
  * (128, 256 or 512 threads per CTA) -- on scratch grids it allocates and
  * frees, records the fastest for (dtype, kind, radius, grid-size class) and
  * returns it with its rate in cell updates per second. The record is used by
- * later iterate calls when the temporal depth (tile height) setting is 0. No
+ * later iterate calls when the temporal depth (tile height) setting is 0; the
+ * settings themselves are left as the caller had them. No
  * reference counterpart (the reference fixes tile width 16,
  * include/muesli.h:195, and 1024-thread blocks, src/muesli.cpp:103). */
 int msl_autotune_stencil2d_shape(int dtype, int kind, int rows, int cols, int radius, int iters, int *best_depth,

@@ -100,7 +100,8 @@ int msl_autotune_stencil2d_shape(int dtype, int kind, int rows, int cols, int ra
     int best = 1, best_rows = 32;
     double best_r = 0.0;
     int rc = MSL_OK;
-    const int saved = 0;
+    // the caller's settings, put back when the trials end
+    const int saved_depth = rt::temporal_depth_setting(), saved_rows = rt::tile_rows_setting();
     // (depth, tile rows); depth 1 is the one-sweep kernel, whose tiles are fixed
     struct Cand {
         int depth, tile_rows;
@@ -150,8 +151,8 @@ int msl_autotune_stencil2d_shape(int dtype, int kind, int rows, int cols, int ra
             best = candidates[k].depth;
             best_rows = candidates[k].tile_rows;
         }
-    msl_set_temporal_depth(saved);
-    msl_set_tile_rows(0);
+    msl_set_temporal_depth(saved_depth);
+    msl_set_tile_rows(saved_rows);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(a);

@@ -59,6 +59,9 @@ int tuned_depth(int dtype, int kind, int rows, int cols, int radius);
 // when none is recorded.
 int tuned_tile_rows(int dtype, int kind, int rows, int cols, int radius);
 
+// msl_set_temporal_depth / msl_set_tile_rows as last set (0: automatic).
+int temporal_depth_setting();
+int tile_rows_setting();
 // heat3D sweeps per launch (msl_set_stencil3d_depth, stencil.cu): nonzero when
 // pairs of sweeps run on the z-marching kernel; its z planes per CTA (0: chosen
 // per grid).

@@ -204,6 +204,8 @@ int depth_for(int dtype, int kind, int rows, int cols, int r) {
 
 namespace msl {
 namespace rt {
+int temporal_depth_setting() { return g_temporal_depth.load(std::memory_order_relaxed); }
+int tile_rows_setting() { return g_tile_rows.load(std::memory_order_relaxed); }
 int stencil3d_pair_sweeps() { return g_depth3d.load(std::memory_order_relaxed) == 2; }
 int stencil3d_zchunk() { return g_zchunk3d.load(std::memory_order_relaxed); }
 }  // namespace rt
