@@ -27,6 +27,15 @@ def test_every_declared_symbol_is_exported(lib):
     assert not missing
 
 
+def test_every_declared_function_has_ctypes_signature(lib):
+    """ctypes passes the arguments of a function without argtypes as C ints,
+    which truncates 64-bit pointers and sizes: the binding must type every
+    entry point the header declares."""
+    untyped = [n for n in abi.declared_functions() if getattr(lib, n).argtypes is None]
+    assert not untyped
+    assert all(getattr(lib, n).restype is not None for n in abi.declared_functions())
+
+
 def test_calls_before_init_report_not_initialized(lib):
     p = ctypes.c_void_p()
     assert lib.msl_alloc(ctypes.byref(p), 16) == abi.MSL_ERR_NOT_INITIALIZED
