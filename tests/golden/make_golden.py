@@ -51,6 +51,31 @@ def save(name, **arrays):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
 
 
+def heat3d_special_case():
+    """heat3D on values around the GPU division's fast-path range: tiny (1e-38)
+    and subnormal (3e-40) cells, +inf cells (never negated, so no sum meets
+    inf - inf and no NaN arises), negative cells; a block of zeros holding
+    single cells at +-2^-122 x {0.999999, 1, 1.25, 1.4999999, 1.5, 1.5000001,
+    2} (a neighbour's first sum is the cell alone) and a block of -0 (the
+    reference's sum starts from +0), both through the whole depth and wide
+    enough that the other values, one cell per sweep, reach neither the
+    single cells nor the -0 block's core within the three sweeps."""
+    rng = np.random.default_rng(58)
+    c = rng.random((16, 40, 70), dtype=np.float32)
+    u = rng.random(c.shape)
+    c[u < 0.01] = np.float32(1e-38)
+    c[(u >= 0.01) & (u < 0.02)] = np.float32(3e-40)
+    c[(u >= 0.02) & (u < 0.025)] = np.float32(np.inf)
+    c[(u >= 0.025) & (u < 0.05)] *= np.float32(-0.3)
+    c[:, 2:22, 2:40] = 0.0
+    t = np.float32(2.0 ** -122)
+    for k, f in enumerate((1.0, 1.25, 1.4999999, 1.5, 1.5000001, 2.0, 0.999999)):
+        c[5 + (k % 2) * 4, 6 + 2 * k, 6 + 5 * k] = np.float32(f) * t * np.float32(1 if k % 2 else -1)
+    c[:, 24:38, 44:62] = np.float32(-0.0)
+    ints = [16, 40, 70, 3]
+    save("dc_heat3d_special", seed=58, ints=ints, in0=c, out=run("dc_heat3d", ints, [c], np.float32, c.size))
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit(f"missing {HARNESS}: run `make -C oracle ref` first")
@@ -119,6 +144,7 @@ def main():
     # DC::mapStencil: heat3D, Dirichlet 0 outside; 3-D box sums (meanblur).
     c = rng(56).random((12, 10, 14), dtype=np.float32)
     save("dc_heat3d", seed=56, ints=[12, 10, 14, 5], in0=c, out=run("dc_heat3d", [12, 10, 14, 5], [c], np.float32, c.size))
+    heat3d_special_case()
     cb = rng(57).random((9, 10, 11), dtype=np.float32)
     for r in (1, 2):
         save(f"dc_boxsum_r{r}", seed=57, ints=[9, 10, 11, r, 1], in0=cb,

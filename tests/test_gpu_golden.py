@@ -66,7 +66,7 @@ def run_on_gpu(A, name, f):
         return A.stencil2d_iterate(A.MSL_ST2_LIFE, dx, out, 1, 0, ints[2], residual=False)[0].download()
     elif name.startswith("dm_boxmean"):
         return A.stencil2d_iterate(A.MSL_ST2_BOXMEAN, dx, out, ints[2], 0.0, ints[3], residual=False)[0].download()
-    elif name == "dc_heat3d":
+    elif name.startswith("dc_heat3d"):
         return A.stencil3d_iterate(A.MSL_ST3_HEAT7, dx, out, 1, 0.0, ints[3], residual=False)[0].download()
     elif name.startswith("dc_boxsum"):
         return A.stencil3d_iterate(A.MSL_ST3_BOXSUM, dx, out, ints[3], 0.0, ints[4], residual=False)[0].download()

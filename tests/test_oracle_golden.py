@@ -105,7 +105,7 @@ def oracle_for(name, f):
         return O.stencil2d_iterate(ST2_LIFE, x, 1, 0, ints[2])[0]
     if name.startswith("dm_boxmean"):
         return O.stencil2d_iterate(ST2_BOXMEAN, x, ints[2], 0.0, ints[3])[0]
-    if name == "dc_heat3d":
+    if name.startswith("dc_heat3d"):
         return O.stencil3d_iterate(ST3_HEAT7, x, 1, 0.0, ints[3])[0]
     if name.startswith("dc_boxsum"):
         return O.stencil3d_iterate(ST3_BOXSUM, x, ints[3], 0.0, ints[4])[0]
